@@ -1,0 +1,328 @@
+"""Throughput of the cone-beam Siddon projection + voxel-driven backprojection pair.
+
+Workload (one step): forward projection A x and backprojection A^T y of the
+512^3 volume over 200x200x150 mm, 360 views over 360 deg, 768x512 detector
+(0.8 mm at SDD 1200, SID 600 -> 0.4 mm at the centre), float32, synthetic
+random-ellipsoid phantom (seed 2).  Metric: GRay/s = rays / (t_FP + t_BP),
+rays = 360 * 768 * 512.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun, one rank per GPU, each rank a full replica of the
+workload (weak scaling: the views of a scan are independent units).
+The reference arm times the reference algorithm's CPU restatement (the FP64
+oracle, OpenMP over all host cores) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "ct-research_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "Gray/s proj+backproj (%HBM roofline)"
+UNIT = "GRay/s"
+WORKLOAD = "cone_512: 512^3 float32 volume (200x200x150 mm), 360 views / 360 deg, 768x512 detector, " \
+           "SID 600 / SDD 1200; one step = Siddon FP + voxel-driven BP"
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _traffic():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    FIELDS = "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def cpu_sample(geom, vol_np, seconds_target=12.0, max_views=32):
+    """Time the oracle's FP + BP on a subset of views (all host threads)."""
+    from oracle.oracle import Oracle
+    o = Oracle(nthreads=os.cpu_count() or 1)
+    g1 = geom.subset_views([7])
+    t0 = time.perf_counter()
+    p = o.cone_fp(vol_np, g1.beta, g1.P, g1.xi, g1.size, g1.D)
+    o.cone_bp(p, g1.beta, g1.P, g1.xi, g1.size, g1.D, g1.vol_shape)
+    t1 = time.perf_counter() - t0
+    nv = int(max(1, min(max_views, seconds_target / max(t1, 1e-3))))
+    idx = np.linspace(0, len(geom.beta) - 1, nv).astype(int)
+    gs = geom.subset_views(idx)
+    t0 = time.perf_counter()
+    p = o.cone_fp(vol_np, gs.beta, gs.P, gs.xi, gs.size, gs.D)
+    o.cone_bp(p, gs.beta, gs.P, gs.xi, gs.size, gs.D, gs.vol_shape)
+    dt = time.perf_counter() - t0
+    rays = gs.n_rays
+    return {"value": rays / dt / 1e9, "unit": UNIT, "cores": o.nthreads, "kind": "port",
+            "sample": f"FP64 oracle FP+BP of {nv} of the 360 views (all 768x512 rays of each view, full "
+                      f"512^3 volume), {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = _dist_env()
+    if rank != 0:
+        return
+    import torch  # noqa: F401  (phantom generation)
+    from ctgb import geometry, phantom
+    geom = geometry.config_cone_512()
+    vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2)).numpy()
+    from oracle.oracle import Oracle
+    o = Oracle(nthreads=os.cpu_count() or 1)
+    # one step = FP + BP of a fixed subset of views (bounded sample of the workload)
+    nv = 2
+    idx = np.linspace(0, len(geom.beta) - 1, nv).astype(int)
+    gs = geom.subset_views(idx)
+
+    def step():
+        p = o.cone_fp(vol, gs.beta, gs.P, gs.xi, gs.size, gs.D)
+        o.cone_bp(p, gs.beta, gs.P, gs.xi, gs.size, gs.D, gs.vol_shape)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    v = gs.n_rays / dt / 1e9
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"{nv} of 360 views per step"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": o.nthreads, "kind": "port",
+                             "sample": f"FP64 oracle (reference algorithm restated in C, OpenMP) FP+BP of {nv} "
+                                       f"of the 360 views per step; the reference's own code is MATLAB + CUDA "
+                                       f"MEX and cannot run on this host"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = _dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    import ctgb
+    from ctgb import geometry, phantom, _lib
+    from ctgb.device import ConePlan
+    ctgb.load()
+    geom = geometry.config_cone_512()
+    vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2), device=dev)
+    plan = ConePlan(geom)
+    proj = plan.new_sino(dev)
+    back = plan.new_volume(dev)
+    stream = torch.cuda.current_stream()
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        plan.fp(vol, proj)
+        if ev:
+            ev[1].record(stream)
+        plan.bp(proj, back)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev.index or 0) as clk:
+        start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    t_total = start.elapsed_time(stop) / 1e3
+    t_fp = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps / 1e3
+    t_bp = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps / 1e3
+    if dist:
+        t = torch.tensor([t_total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    t_step = t_total / args.steps
+    value = world * geom.n_rays / t_step / 1e9
+
+    # e2e through the C ABI with host (pinned) buffers: copies inside the timed region
+    import ctypes as C
+    h_vol = torch.empty(geom.vol_shape, dtype=torch.float32, pin_memory=True)
+    h_vol.copy_(vol.cpu())
+    h_proj = torch.empty(geom.sino_shape, dtype=torch.float32, pin_memory=True)
+    h_back = torch.empty(geom.vol_shape, dtype=torch.float32, pin_memory=True)
+    lib = _lib.lib()
+    res = np.array([geom.size[0] / geom.nt, geom.size[1] / geom.ns, geom.size[2] / geom.nz])
+    size = np.array(geom.size)
+    vp = lambda a: C.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else C.c_void_p(a.data_ptr())
+
+    def e2e_step():
+        _lib.check(lib.ct_ProjectionCone_3D(vp(h_vol), vp(h_proj), vp(geom.beta), vp(geom.P), vp(geom.xi),
+                                            geom.nt, geom.ns, geom.nz, size[0] / 2, size[1] / 2, size[2] / 2,
+                                            len(geom.beta), len(geom.P), len(geom.xi), geom.D, vp(res)),
+                   "ct_ProjectionCone_3D")
+        _lib.check(lib.ct_BackPro(vp(h_back), vp(h_proj), vp(geom.xi), vp(geom.P), vp(geom.beta), geom.D,
+                                  len(geom.beta), len(geom.P), len(geom.xi), vp(size), geom.nt, geom.ns, geom.nz),
+                   "ct_BackPro")
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": world * geom.n_rays / t_e2e / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_vol.numel() * 4 + h_proj.numel() * 4),
+           "d2h_bytes_per_step": int(h_proj.numel() * 4 + h_back.numel() * 4),
+           "ms_per_step": t_e2e * 1e3}
+
+    if rank != 0:
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    segs = plan.count_segments()
+    R, V, B = geom.n_rays, geom.n_voxels, len(geom.beta)
+    fp_bytes = 4 * segs + 4 * R
+    bp_bytes = 16 * V * B + 8 * V
+    peak, peak_kind = _peaks()
+    traffic = _traffic()
+    kern = {
+        "cone_fp_kernel": {"ms": t_fp * 1e3, "algorithmic_bytes": fp_bytes,
+                           "achieved_gbs": fp_bytes / t_fp / 1e9, "segments": segs},
+        "cone_bp_kernel+pack_quads": {"ms": t_bp * 1e3, "algorithmic_bytes": bp_bytes,
+                                      "achieved_gbs": bp_bytes / t_bp / 1e9},
+    }
+    dom = "cone_fp_kernel" if t_fp >= t_bp else "cone_bp_kernel+pack_quads"
+    ach = kern[dom]["achieved_gbs"]
+    tr = traffic.get(dom.split("+")[0])
+    roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": tr, "kernel": dom, "peak_source": peak_kind,
+                "pair_frac": (fp_bytes + bp_bytes) / (t_fp + t_bp) / 1e9 / peak}
+    cpu = cpu_sample(geom, vol.cpu().numpy()) if (world == 1 and not args.no_cpu) else None
+    clocks = clk.summary()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (512 MiB volume, 566 MB sinogram, 2.3 GB packed quads)",
+                       "phantom": "12 random ellipsoids, seed 2"},
+            "roofline": roofline, "kernels": kern, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 3 * args.steps}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

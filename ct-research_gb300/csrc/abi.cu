@@ -1,0 +1,633 @@
+// abi.cu -- the C ABI of libctgb.so (declared in include/ctgb.h).
+//
+// Plans hold the geometry in HBM (per-view trig tables, detector domains,
+// filter taps, pre-weight tables) and lazily grown workspaces.  The drop-in
+// host-pointer entry points keep the argument lists of the reference host
+// helpers; they stage host data through device buffers that persist between
+// calls (the reference allocates, copies and resets the device on every call,
+// ProjectionCone_3D.cu:433-520 and ProjectionCone_3D.cpp:53).
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace ct {
+
+
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int cuda_status(cudaError_t e, const char *what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    (void)cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? CT_ERR_OOM : CT_ERR_CUDA;
+}
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// Device buffer that grows on demand.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n) {
+        if (n <= bytes) return CT_OK;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        CT_CUDA(cudaMalloc(&ptr, n), "cudaMalloc");
+        bytes = n;
+        return CT_OK;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(ptr); }
+};
+
+template <typename T>
+static int upload(DevBuf &b, const T *host, size_t n) {
+    int s = b.ensure(sizeof(T) * n);
+    if (s) return s;
+    CT_CUDA(cudaMemcpy(b.ptr, host, sizeof(T) * n, cudaMemcpyHostToDevice), "upload");
+    return CT_OK;
+}
+
+// Shepp-Logan-form taps exactly as GFunction computes them (FDK.cu:6-19):
+// double arithmetic, stored as float.
+static std::vector<float> sl_taps(float pint, int np) {
+    const double PI = 3.141592653589793;
+    std::vector<float> g(2 * (size_t)np - 1);
+    for (int n = 0; n < np; ++n) {
+        if (n == 0) {
+            g[np - 1] = (float)(1.0 / (1.0 * (PI * pint) * (PI * pint)));
+        } else {
+            const double a = 1.0 * ((double)pint * PI) * ((double)pint * PI);
+            const double v = -1.0 / a / (4 * (1.0 * n * n) - 1);
+            g[np - 1 - n] = g[np - 1 + n] = (float)v;
+        }
+    }
+    return g;
+}
+
+}  // namespace ct
+
+using namespace ct;
+
+// ---------------------------------------------------------------------------
+// cone plan
+// ---------------------------------------------------------------------------
+struct ct_cone_plan {
+    ConeGeom g{};
+    DevBuf trig, P, xi;
+    DevBuf quads, rcov, G, wtab, norms;
+    int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
+    int fdk_bp = CT_FDK_BP_STICKY;
+    // host copies of the geometry (drop-in cache key)
+    std::vector<float> hb, hp, hx;
+    double hsize[3] = {0, 0, 0};
+    ~ct_cone_plan() {
+        trig.release(); P.release(); xi.release();
+        quads.release(); rcov.release(); G.release(); wtab.release(); norms.release();
+    }
+};
+
+static int check_domain(const float *a, int n, const char *what) {
+    if (!a) { set_error(std::string(what) + ": null"); return CT_ERR_ARG; }
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) { set_error(std::string(what) + ": non-finite value"); return CT_ERR_ARG; }
+    return CT_OK;
+}
+
+extern "C" {
+
+const char *ct_last_error(void) { return g_last_error.c_str(); }
+const char *ct_version(void) { return "ctgb 0.1 (sm_103a)"; }
+
+int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double *Size, const float *beta,
+                        int nb, const float *P, int np, const float *xi, int nx, double D) {
+    CT_REQUIRE(out, "plan pointer is null");
+    *out = nullptr;
+    CT_REQUIRE(nt > 0 && ns > 0 && nz > 0, "volume sizes must be positive");
+    CT_REQUIRE((long long)nt * ns * nz < (1LL << 31), "volume larger than 2^31 voxels");
+    CT_REQUIRE(nb > 0 && nb <= 65535, "number of views must be in [1, 65535]");
+    CT_REQUIRE(np > 0 && nx > 0, "detector sizes must be positive");
+    CT_REQUIRE((long long)nb * np * nx < (1LL << 40), "sinogram too large");
+    CT_REQUIRE(Size && Size[0] > 0 && Size[1] > 0 && Size[2] > 0, "Size must be positive");
+    CT_REQUIRE(D > 0.5 * std::sqrt(Size[0] * Size[0] + Size[1] * Size[1]),
+               "Distance must exceed the in-plane half diagonal of the volume");
+    int s;
+    if ((s = check_domain(beta, nb, "BetaScanRange")) || (s = check_domain(P, np, "Pdomain")) ||
+        (s = check_domain(xi, nx, "Xigamadomain")))
+        return s;
+    ct_cone_plan *pl = new ct_cone_plan();
+    ConeGeom &g = pl->g;
+    g.nt = nt; g.ns = ns; g.nz = nz;
+    g.nb = nb; g.np = np; g.nx = nx;
+    for (int a = 0; a < 3; ++a) g.size[a] = Size[a];
+    g.res[0] = 1.0 * Size[0] / nt;
+    g.res[1] = 1.0 * Size[1] / ns;
+    g.res[2] = 1.0 * Size[2] / nz;
+    g.D = D;
+    // float-range bookkeeping of BackPro / FDKpro (Backprojection3D.cu:304-311)
+    g.pint = np > 1 ? std::fabs(P[1] - P[0]) : 1.0f;
+    g.xint = nx > 1 ? std::fabs(xi[1] - xi[0]) : 1.0f;
+    g.bint = nb > 1 ? std::fabs(beta[1] - beta[0]) : 0.0f;
+    g.maxp = std::max(P[0], P[np - 1]);
+    g.minp = std::min(P[0], P[np - 1]);
+    g.maxx = std::max(xi[0], xi[nx - 1]);
+    g.minx = std::min(xi[0], xi[nx - 1]);
+    g.p0 = P[0];
+    g.x0 = xi[0];
+    g.psgn = (np > 1 && P[np - 1] < P[0]) ? -1.0f : 1.0f;
+    g.xsgn = (nx > 1 && xi[nx - 1] < xi[0]) ? -1.0f : 1.0f;
+    // the reference evaluates sin/cos of the float angle with the
+    // single-precision overloads (ProjectionCone_3D.cu:26-28)
+    std::vector<double2> tr(nb);
+    for (int v = 0; v < nb; ++v) tr[v] = make_double2((double)sinf(beta[v]), (double)cosf(beta[v]));
+    if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->P, P, np)) || (s = upload(pl->xi, xi, nx))) {
+        delete pl;
+        return s;
+    }
+    g.trig = pl->trig.as<double2>();
+    g.P = pl->P.as<float>();
+    g.xi = pl->xi.as<float>();
+    pl->hb.assign(beta, beta + nb);
+    pl->hp.assign(P, P + np);
+    pl->hx.assign(xi, xi + nx);
+    for (int a = 0; a < 3; ++a) pl->hsize[a] = Size[a];
+    *out = pl;
+    return CT_OK;
+}
+
+int ct_cone_plan_destroy(ct_cone_plan *plan) {
+    delete plan;
+    return CT_OK;
+}
+
+int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode) {
+    CT_REQUIRE(plan, "plan is null");
+    CT_REQUIRE(filter_mode == 0 || filter_mode == 1, "filter_mode must be 0 or 1");
+    CT_REQUIRE(bp_mode == 0 || bp_mode == 1, "bp_mode must be 0 or 1");
+    plan->fdk_filter = filter_mode;
+    plan->fdk_bp = bp_mode;
+    return CT_OK;
+}
+
+size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
+    if (!plan) return 0;
+    return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes;
+}
+
+int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stream) {
+    CT_REQUIRE(plan && d_vol && d_proj, "ct_cone_fp: null argument");
+    return cone_fp_launch(plan->g, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, as_stream(stream));
+}
+
+int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b, const float *d_rowsum,
+                        float eps, float *d_out, double *d_norms, void *stream) {
+    CT_REQUIRE(plan && d_vol && d_b && d_out && d_norms, "ct_cone_fp_residual: null argument");
+    return cone_fp_launch(plan->g, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, as_stream(stream));
+}
+
+static int cone_bp_common(ct_cone_plan *plan, const float *d_proj, float *d_vol, int weighting,
+                          const float *colsum, float eps, float lambda, float lo, float hi, bool update,
+                          cudaStream_t st) {
+    int s = plan->quads.ensure(cone_quads_bytes(plan->g));
+    if (s) return s;
+    if ((s = cone_pack_quads(plan->g, d_proj, plan->quads.as<float4>(), st))) return s;
+    return cone_bp_launch(plan->g, plan->quads.as<float4>(), d_vol, weighting, colsum, eps, lambda, lo, hi,
+                          update, st);
+}
+
+int ct_cone_bp(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_vol, "ct_cone_bp: null argument");
+    CT_REQUIRE(plan->g.np >= 2 && plan->g.nx >= 2, "ct_cone_bp: detector needs at least 2x2 samples");
+    return cone_bp_common(plan, d_proj, d_vol, 0, nullptr, 0.f, 0.f, 0.f, 0.f, false, as_stream(stream));
+}
+
+int ct_cone_bp_update(ct_cone_plan *plan, const float *d_proj, const float *d_colsum, float eps, float lambda,
+                      float lo, float hi, float *d_vol, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_colsum && d_vol, "ct_cone_bp_update: null argument");
+    CT_REQUIRE(plan->g.np >= 2 && plan->g.nx >= 2, "ct_cone_bp_update: detector needs at least 2x2 samples");
+    return cone_bp_common(plan, d_proj, d_vol, 0, d_colsum, eps, lambda, lo, hi, true, as_stream(stream));
+}
+
+int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_vol, "ct_cone_fdk: null argument");
+    ConeGeom &g = plan->g;
+    CT_REQUIRE(g.np >= 2 && g.nx >= 2, "ct_cone_fdk: detector needs at least 2x2 samples");
+    cudaStream_t st = as_stream(stream);
+    int s;
+    if (!plan->G.ptr) {
+        std::vector<float> taps = sl_taps(g.pint, g.np);
+        if ((s = upload(plan->G, taps.data(), taps.size()))) return s;
+        // pre-weight D / sqrt(D^2 + P^2 + xi^2) per (xi, P), in double (FDK.cu:34)
+        std::vector<double> w((size_t)g.nx * g.np);
+        for (int x = 0; x < g.nx; ++x)
+            for (int p = 0; p < g.np; ++p) {
+                const double Pv = plan->hp[p], Xv = plan->hx[x];
+                w[(size_t)x * g.np + p] = g.D / std::sqrt(1.0 * g.D * g.D + 1.0 * Pv * Pv + 1.0 * Xv * Xv);
+            }
+        if ((s = upload(plan->wtab, w.data(), w.size()))) return s;
+    }
+    if ((s = plan->rcov.ensure(sizeof(float) * (size_t)g.nb * g.nx * g.np))) return s;
+    RowFilter f{};
+    f.nrow = g.nb * g.nx;
+    f.np = g.np;
+    f.pint = g.pint;
+    f.G = plan->G.as<float>();
+    f.w = plan->wtab.as<double>();
+    f.wrows = g.nx;
+    f.launch_order = plan->fdk_filter;
+    f.tile = 256;        // FDK.h:22 threadX
+    f.limit = 2048;      // FDK.h:24 Filterlengthlimit
+    f.row_block = 256;   // FDK.h:23 blockX
+    f.rowmod = g.nx;
+    if ((s = row_filter_launch(f, d_proj, plan->rcov.as<float>(), st))) return s;
+    return cone_bp_common(plan, plan->rcov.as<float>(), d_vol, plan->fdk_bp == CT_FDK_BP_STICKY ? 2 : 1,
+                          nullptr, 0.f, 0.f, 0.f, 0.f, false, st);
+}
+
+int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream) {
+    CT_REQUIRE(plan && segments, "ct_cone_count_segments: null argument");
+    cudaStream_t st = as_stream(stream);
+    int s = plan->norms.ensure(2 * sizeof(double));
+    if (s) return s;
+    CT_CUDA(cudaMemsetAsync(plan->norms.ptr, 0, 2 * sizeof(double), st), "memset");
+    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, st)))
+        return s;
+    double h = 0;
+    CT_CUDA(cudaMemcpyAsync(&h, plan->norms.ptr, sizeof(double), cudaMemcpyDeviceToHost, st), "copy");
+    CT_CUDA(cudaStreamSynchronize(st), "sync");
+    *segments = (long long)llround(h);
+    return CT_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// fan plan (2D fan and parallel beam)
+// ---------------------------------------------------------------------------
+struct ct_fan_plan {
+    FanGeom g{};
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov;
+    std::vector<float> hPf;
+    ~ct_fan_plan() {
+        trig_d.release(); Pd.release(); trig_f.release(); Pf.release();
+        G.release(); wtab.release(); rcov.release();
+    }
+};
+
+// size2 = extents (fastest axis first), ang/P double; angles and bins are
+// rounded to float for the backprojectors as the MATLAB callers do (single()).
+static int fan_plan_make(ct_fan_plan **out, int nt, int ns, const double size2[2], const double *ang, int nb,
+                         const double *P, int np, double D, int parallel) {
+    CT_REQUIRE(out, "plan pointer is null");
+    *out = nullptr;
+    CT_REQUIRE(nt > 0 && ns > 0, "image sizes must be positive");
+    CT_REQUIRE((long long)nt * ns < (1LL << 31), "image too large");
+    CT_REQUIRE(nb > 0 && np > 0, "sinogram sizes must be positive");
+    CT_REQUIRE(size2[0] > 0 && size2[1] > 0, "Size must be positive");
+    CT_REQUIRE(ang && P, "null domain");
+    if (!parallel)
+        CT_REQUIRE(D > 0.5 * std::sqrt(size2[0] * size2[0] + size2[1] * size2[1]),
+                   "Distance must exceed the half diagonal of the image");
+    for (int i = 0; i < nb; ++i) CT_REQUIRE(std::isfinite(ang[i]), "non-finite angle");
+    for (int i = 0; i < np; ++i) CT_REQUIRE(std::isfinite(P[i]), "non-finite detector coordinate");
+    ct_fan_plan *pl = new ct_fan_plan();
+    FanGeom &g = pl->g;
+    g.nt = nt; g.ns = ns; g.nb = nb; g.np = np;
+    g.size[0] = size2[0]; g.size[1] = size2[1];
+    g.res[0] = 1.0 * size2[0] / nt;
+    g.res[1] = 1.0 * size2[1] / ns;
+    g.D = D;
+    g.parallel = parallel;
+    g.smax = std::max(std::fabs(P[0]), std::fabs(P[np - 1]));
+    std::vector<double2> td(nb);
+    std::vector<float2> tf(nb);
+    std::vector<float> pf(np), bf(nb);
+    for (int v = 0; v < nb; ++v) {
+        td[v] = make_double2(std::sin(ang[v]), std::cos(ang[v]));
+        bf[v] = (float)ang[v];
+        tf[v] = make_float2(sinf(bf[v]), cosf(bf[v]));
+    }
+    for (int p = 0; p < np; ++p) pf[p] = (float)P[p];
+    g.pint = np > 1 ? std::fabs(pf[1] - pf[0]) : 1.0f;
+    g.bint = nb > 1 ? std::fabs(bf[1] - bf[0]) : 0.0f;
+    g.maxp = std::max(pf[0], pf[np - 1]);
+    g.minp = std::min(pf[0], pf[np - 1]);
+    g.p0 = pf[0];
+    g.psgn = (np > 1 && pf[np - 1] < pf[0]) ? -1.0f : 1.0f;
+    int s;
+    if ((s = upload(pl->trig_d, td.data(), nb)) || (s = upload(pl->Pd, P, np)) ||
+        (s = upload(pl->trig_f, tf.data(), nb)) || (s = upload(pl->Pf, pf.data(), np))) {
+        delete pl;
+        return s;
+    }
+    g.trig_d = pl->trig_d.as<double2>();
+    g.Pd = pl->Pd.as<double>();
+    g.trig_f = pl->trig_f.as<float2>();
+    g.Pf = pl->Pf.as<float>();
+    pl->hPf = pf;
+    *out = pl;
+    return CT_OK;
+}
+
+extern "C" {
+
+int ct_fan_plan_create(ct_fan_plan **plan, int nt, int ns, const double *Size, const double *beta, int nb,
+                       const double *P, int np, double D) {
+    CT_REQUIRE(Size, "Size is null");
+    return fan_plan_make(plan, nt, ns, Size, beta, nb, P, np, D, 0);
+}
+
+int ct_fan_plan_destroy(ct_fan_plan *plan) {
+    delete plan;
+    return CT_OK;
+}
+
+int ct_fan_fp(ct_fan_plan *plan, const float *d_img, float *d_proj, void *stream) {
+    CT_REQUIRE(plan && d_img && d_proj, "ct_fan_fp: null argument");
+    return fan_fp_launch(plan->g, d_img, d_proj, nullptr, nullptr, 0.f, nullptr, 0, as_stream(stream));
+}
+
+int ct_fan_fp_residual(ct_fan_plan *plan, const float *d_img, const float *d_b, const float *d_rowsum, float eps,
+                       float *d_out, double *d_norms, void *stream) {
+    CT_REQUIRE(plan && d_img && d_b && d_out && d_norms, "ct_fan_fp_residual: null argument");
+    return fan_fp_launch(plan->g, d_img, d_out, d_b, d_rowsum, eps, d_norms, 1, as_stream(stream));
+}
+
+int ct_fan_bp(ct_fan_plan *plan, const float *d_proj, float *d_img, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_img, "ct_fan_bp: null argument");
+    return fan_bp_launch(plan->g, d_proj, d_img, plan->g.parallel ? 2 : 0, nullptr, 0.f, 0.f, 0.f, 0.f, false,
+                         as_stream(stream));
+}
+
+int ct_fan_bp_update(ct_fan_plan *plan, const float *d_proj, const float *d_colsum, float eps, float lambda,
+                     float lo, float hi, float *d_img, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_colsum && d_img, "ct_fan_bp_update: null argument");
+    return fan_bp_launch(plan->g, d_proj, d_img, 0, d_colsum, eps, lambda, lo, hi, true, as_stream(stream));
+}
+
+// FBP of a 2D fan (FBPfan.cu) or parallel (FBPparallel.cu) sinogram.
+int ct_fan_fbp(ct_fan_plan *plan, const float *d_proj, float *d_img, int filter_mode, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_img, "ct_fan_fbp: null argument");
+    FanGeom &g = plan->g;
+    CT_REQUIRE(g.np >= 2, "ct_fan_fbp: at least 2 detector bins");
+    cudaStream_t st = as_stream(stream);
+    int s;
+    if (!plan->G.ptr) {
+        std::vector<float> taps = sl_taps(g.pint, g.np);
+        if ((s = upload(plan->G, taps.data(), taps.size()))) return s;
+        if (!g.parallel) {
+            std::vector<double> w(g.np);   // Rscan / sqrt(Rscan^2 + P^2) (FBPfan.cu:32)
+            for (int p = 0; p < g.np; ++p) {
+                const double Pv = plan->hPf[p];
+                w[p] = g.D / std::sqrt(1.0 * g.D * g.D + 1.0 * Pv * Pv);
+            }
+            if ((s = upload(plan->wtab, w.data(), w.size()))) return s;
+        }
+    }
+    if ((s = plan->rcov.ensure(sizeof(float) * (size_t)g.nb * g.np))) return s;
+    RowFilter f{};
+    f.nrow = g.nb;
+    f.np = g.np;
+    f.pint = g.pint;
+    f.G = plan->G.as<float>();
+    f.w = g.parallel ? nullptr : plan->wtab.as<double>();
+    f.wrows = 1;
+    f.launch_order = filter_mode;
+    f.tile = g.parallel ? 256 : 128;          // FBPparallel.h:24 / FBPfan.h:24
+    f.limit = g.parallel ? 2048 : 1024;       // FBPparallel.h:26 / FBPfan.h:26
+    f.row_block = g.parallel ? 256 : 128;
+    f.rowmod = g.nb;
+    if ((s = row_filter_launch(f, d_proj, plan->rcov.as<float>(), st))) return s;
+    return fan_bp_launch(g, plan->rcov.as<float>(), d_img, g.parallel ? 2 : 1, nullptr, 0.f, 0.f, 0.f, 0.f, false,
+                         st);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Drop-in host-pointer entry points
+// ---------------------------------------------------------------------------
+namespace {
+
+std::mutex g_dropin_mutex;
+
+struct DropinState {
+    ct_cone_plan *cone = nullptr;
+    DevBuf vol, proj;
+};
+DropinState &dropin() {
+    static DropinState st;
+    return st;
+}
+
+// Reuse the cached cone plan when the geometry is unchanged.
+int cached_cone_plan(ct_cone_plan **out, int nt, int ns, int nz, const double *Size, const float *beta, int nb,
+                     const float *P, int np, const float *xi, int nx, double D) {
+    DropinState &st = dropin();
+    ct_cone_plan *pl = st.cone;
+    if (pl && pl->g.nt == nt && pl->g.ns == ns && pl->g.nz == nz && pl->g.nb == nb && pl->g.np == np &&
+        pl->g.nx == nx && pl->g.D == D && pl->hsize[0] == Size[0] && pl->hsize[1] == Size[1] &&
+        pl->hsize[2] == Size[2] && !std::memcmp(pl->hb.data(), beta, sizeof(float) * nb) &&
+        !std::memcmp(pl->hp.data(), P, sizeof(float) * np) && !std::memcmp(pl->hx.data(), xi, sizeof(float) * nx)) {
+        *out = pl;
+        return CT_OK;
+    }
+    ct_cone_plan *np_ = nullptr;
+    int s = ct_cone_plan_create(&np_, nt, ns, nz, Size, beta, nb, P, np, xi, nx, D);
+    if (s) return s;
+    if (st.cone) ct_cone_plan_destroy(st.cone);
+    st.cone = np_;
+    *out = np_;
+    return CT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaScanRange, const float *Pdomain,
+                         const float *Xigamadomain, int t_length, int s_length, int z_length, double Center_t,
+                         double Center_s, double Center_z, int LBeta, int LP, int LXigama, double Distance,
+                         const double *resolution) {
+    CT_REQUIRE(Pic && Projection && resolution, "ct_ProjectionCone_3D: null argument");
+    std::lock_guard<std::mutex> lk(g_dropin_mutex);
+    // the gateway passes Center = Size/2 and resolution = Size/length (ProjectionCone_3D.cpp:10-22)
+    const double Size[3] = {resolution[0] * t_length, resolution[1] * s_length, resolution[2] * z_length};
+    CT_REQUIRE(std::fabs(Center_t - 0.5 * Size[0]) <= 1e-9 * Size[0] &&
+                   std::fabs(Center_s - 0.5 * Size[1]) <= 1e-9 * Size[1] &&
+                   std::fabs(Center_z - 0.5 * Size[2]) <= 1e-9 * Size[2],
+               "ct_ProjectionCone_3D: the rotation centre must be the volume centre");
+    ct_cone_plan *pl;
+    int s = cached_cone_plan(&pl, t_length, s_length, z_length, Size, BetaScanRange, LBeta, Pdomain, LP,
+                             Xigamadomain, LXigama, Distance);
+    if (s) return s;
+    // keep the exact resolution the caller passed
+    for (int a = 0; a < 3; ++a) pl->g.res[a] = resolution[a];
+    DropinState &st = dropin();
+    const size_t nv = (size_t)t_length * s_length * z_length, npj = (size_t)LBeta * LP * LXigama;
+    if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;
+    CT_CUDA(cudaMemcpy(st.vol.ptr, Pic, nv * sizeof(float), cudaMemcpyHostToDevice), "H2D volume");
+    if ((s = ct_cone_fp(pl, st.vol.as<float>(), st.proj.as<float>(), nullptr))) return s;
+    CT_CUDA(cudaMemcpy(Projection, st.proj.ptr, npj * sizeof(float), cudaMemcpyDeviceToHost), "D2H projection");
+    return CT_OK;
+}
+
+static int cone_bp_dropin(float *Display, const float *R, const float *xi, const float *P, const float *beta,
+                          double D, int nb, int np, int nx, const double *Size, int nt, int ns, int nz, bool fdk) {
+    CT_REQUIRE(Display && R && Size, "null argument");
+    std::lock_guard<std::mutex> lk(g_dropin_mutex);
+    ct_cone_plan *pl;
+    int s = cached_cone_plan(&pl, nt, ns, nz, Size, beta, nb, P, np, xi, nx, D);
+    if (s) return s;
+    DropinState &st = dropin();
+    const size_t nv = (size_t)nt * ns * nz, npj = (size_t)nb * np * nx;
+    if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;
+    CT_CUDA(cudaMemcpy(st.proj.ptr, R, npj * sizeof(float), cudaMemcpyHostToDevice), "H2D projection");
+    s = fdk ? ct_cone_fdk(pl, st.proj.as<float>(), st.vol.as<float>(), nullptr)
+            : ct_cone_bp(pl, st.proj.as<float>(), st.vol.as<float>(), nullptr);
+    if (s) return s;
+    CT_CUDA(cudaMemcpy(Display, st.vol.ptr, nv * sizeof(float), cudaMemcpyDeviceToHost), "D2H volume");
+    return CT_OK;
+}
+
+int ct_BackPro(float *Display, const float *R, const float *Xigamadomain, const float *Pdomain,
+               const float *BetaScanRange, double Distance, int LBeta, int LP, int LXigama, const double *Size,
+               int t_length, int s_length, int z_length) {
+    return cone_bp_dropin(Display, R, Xigamadomain, Pdomain, BetaScanRange, Distance, LBeta, LP, LXigama, Size,
+                          t_length, s_length, z_length, false);
+}
+
+int ct_FDKpro(float *Display, const float *R, const float *Xigamadomain, const float *Pdomain,
+              const float *BetaScanRange, double Distance, int LBeta, int LP, int LXigama, const double *Size,
+              int t_length, int s_length, int z_length) {
+    return cone_bp_dropin(Display, R, Xigamadomain, Pdomain, BetaScanRange, Distance, LBeta, LP, LXigama, Size,
+                          t_length, s_length, z_length, true);
+}
+
+// 2D entry points: small problems, a plan per call.
+static int fan2d_run(ct_fan_plan *pl, int which, const void *in, void *out, int filter_mode) {
+    FanGeom &g = pl->g;
+    const size_t nimg = (size_t)g.nt * g.ns, nsino = (size_t)g.nb * g.np;
+    DevBuf a, b;
+    int s = 0;
+    const bool fp = which == 0;
+    if ((s = a.ensure((fp ? nimg : nsino) * sizeof(float))) ||
+        (s = b.ensure((fp ? nsino * sizeof(double) : nimg * sizeof(float))))) {
+        a.release();
+        b.release();
+        return s;
+    }
+    cudaError_t e = cudaMemcpy(a.ptr, in, (fp ? nimg : nsino) * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) s = cuda_status(e, "H2D");
+    if (!s) {
+        if (fp) s = fan_fp_launch(g, a.as<float>(), b.ptr, nullptr, nullptr, 0.f, nullptr, 3, 0);
+        else if (which == 1) s = fan_bp_launch(g, a.as<float>(), b.as<float>(), 0, nullptr, 0, 0, 0, 0, false, 0);
+        else s = ct_fan_fbp(pl, a.as<float>(), b.as<float>(), filter_mode, nullptr);
+    }
+    if (!s) {
+        e = cudaMemcpy(out, b.ptr, fp ? nsino * sizeof(double) : nimg * sizeof(float), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) s = cuda_status(e, "D2H");
+    }
+    a.release();
+    b.release();
+    return s;
+}
+
+int ct_ProjectionFan_2D(const float *Pic, double *Projection, const double *BetaScanRange, const double *Pdomain,
+                        int t_length, int s_length, double Center_t, double Center_s, int LBeta, int LP,
+                        double Distance, const double *resolution) {
+    CT_REQUIRE(Pic && Projection && resolution, "ct_ProjectionFan_2D: null argument");
+    const double size2[2] = {resolution[0] * t_length, resolution[1] * s_length};
+    CT_REQUIRE(std::fabs(Center_t - 0.5 * size2[0]) <= 1e-9 * size2[0] &&
+                   std::fabs(Center_s - 0.5 * size2[1]) <= 1e-9 * size2[1],
+               "ct_ProjectionFan_2D: the rotation centre must be the image centre");
+    ct_fan_plan *pl;
+    int s = fan_plan_make(&pl, t_length, s_length, size2, BetaScanRange, LBeta, Pdomain, LP, Distance, 0);
+    if (s) return s;
+    pl->g.res[0] = resolution[0];
+    pl->g.res[1] = resolution[1];
+    s = fan2d_run(pl, 0, Pic, Projection, 0);
+    ct_fan_plan_destroy(pl);
+    return s;
+}
+
+int ct_ProjectionParallel_2D(const float *Pic, double *Projection, const double *thetaRange, const double *t_Range,
+                             int height, int width, double Center_y, double Center_x, int Ltheta, int Lt,
+                             const double *resolution) {
+    CT_REQUIRE(Pic && Projection && resolution, "ct_ProjectionParallel_2D: null argument");
+    // x runs along width (resolution[1]), y along height (resolution[0]); pixel y*width + x
+    const double size2[2] = {resolution[1] * width, resolution[0] * height};
+    CT_REQUIRE(std::fabs(Center_x - 0.5 * size2[0]) <= 1e-9 * size2[0] &&
+                   std::fabs(Center_y - 0.5 * size2[1]) <= 1e-9 * size2[1],
+               "ct_ProjectionParallel_2D: the rotation centre must be the image centre");
+    ct_fan_plan *pl;
+    int s = fan_plan_make(&pl, width, height, size2, thetaRange, Ltheta, t_Range, Lt, 0.0, 1);
+    if (s) return s;
+    pl->g.res[0] = resolution[1];
+    pl->g.res[1] = resolution[0];
+    s = fan2d_run(pl, 0, Pic, Projection, 0);
+    ct_fan_plan_destroy(pl);
+    return s;
+}
+
+static int fan_plan_from_float(ct_fan_plan **pl, const float *P, const float *beta, int nb, int np, const double *Size,
+                               int nt, int ns, double D, int parallel) {
+    CT_REQUIRE(P && beta && Size, "null argument");
+    std::vector<double> bd(beta, beta + nb), pd(P, P + np);
+    return fan_plan_make(pl, nt, ns, Size, bd.data(), nb, pd.data(), np, D, parallel);
+}
+
+int ct_BackprojectionFan2D(float *Display, const float *R, const float *Pdomain, const float *BetaScanRange,
+                           int LBeta, int LP, const double *Size, int t_length, int s_length, double Rscan) {
+    CT_REQUIRE(Display && R, "ct_BackprojectionFan2D: null argument");
+    ct_fan_plan *pl;
+    int s = fan_plan_from_float(&pl, Pdomain, BetaScanRange, LBeta, LP, Size, t_length, s_length, Rscan, 0);
+    if (s) return s;
+    s = fan2d_run(pl, 1, R, Display, 0);
+    ct_fan_plan_destroy(pl);
+    return s;
+}
+
+int ct_FBPfan(float *Display, const float *R, const float *Pdomain, const float *BetaScanRange, int LBeta, int LP,
+              const double *Size, int t_length, int s_length, double Rscan) {
+    CT_REQUIRE(Display && R, "ct_FBPfan: null argument");
+    ct_fan_plan *pl;
+    int s = fan_plan_from_float(&pl, Pdomain, BetaScanRange, LBeta, LP, Size, t_length, s_length, Rscan, 0);
+    if (s) return s;
+    s = fan2d_run(pl, 2, R, Display, CT_FDK_FILTER_LAUNCH_ORDER);
+    ct_fan_plan_destroy(pl);
+    return s;
+}
+
+int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float *ThetaScanRange, int LTheta, int LT,
+               const double *Size, int t_length, int s_length) {
+    CT_REQUIRE(Display && R, "ct_FBPpara: null argument");
+    ct_fan_plan *pl;
+    int s = fan_plan_from_float(&pl, Tdomain, ThetaScanRange, LTheta, LT, Size, t_length, s_length, 0.0, 1);
+    if (s) return s;
+    s = fan2d_run(pl, 2, R, Display, 0);
+    ct_fan_plan_destroy(pl);
+    return s;
+}
+
+}  // extern "C"

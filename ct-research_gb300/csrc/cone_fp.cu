@@ -1,0 +1,97 @@
+// cone_fp.cu -- cone-beam Siddon forward projection for sm_103a.
+//
+// One thread per ray (beta, xi, P).  The ray geometry is that of
+// ProjectionCone (ProjectionCone_3D.cu:25-42): source at
+// (C_t - D sin b, C_s + D cos b, C_z), ray through the virtual detector point
+// P*u + xi*e_z on the plane through the rotation centre, so its direction is
+// d = (P cos b + D sin b, P sin b - D cos b, xi).
+//
+// The reference walks the grid by comparing squared distances to the next
+// t, s and z planes in FP64 and assigns each segment to the voxel holding its
+// midpoint (:270-375).  Here the same segments are produced by an
+// alpha-parameter Siddon walk: the entry and exit parameters and the entry /
+// exit voxels come from an FP64 slab test (the only FP64 step: voxel
+// assignment at the box boundary needs it), then the walk runs in FP32
+// registers (siddon.cuh).  The walk is unrolled by four so four gathers are
+// in flight per thread.
+#include "cone_geom.cuh"
+#include "siddon.cuh"
+
+namespace ct {
+
+namespace {
+
+constexpr int FP_BX = 32;   // detector columns per block (one warp)
+constexpr int FP_BY = 4;    // detector rows per block
+
+// Source and direction of ray (v, p, x): ProjectionCone_3D.cu:25-42.
+__device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x, RayWalk &w) {
+    const double2 tr = g.trig[v];
+    const double sb = tr.x, cb = tr.y;
+    const double D = g.D;
+    const double Pd = (double)g.P[p], Xd = (double)g.xi[x];
+    const double src[3] = {0.5 * g.size[0] - D * sb, 0.5 * g.size[1] + D * cb, 0.5 * g.size[2]};
+    const double d[3] = {Pd * cb + D * sb, Pd * sb - D * cb, Xd};
+    const int n[3] = {g.nt, g.ns, g.nz};
+    return siddon_setup(src, d, n, g.res, w);
+}
+
+// MODE 0: proj = A vol.  MODE 1: out = (b - A vol) * scale, norms += (|r|^2, |b|^2).
+// MODE 2: count segments into *norms (as double).
+template <int MODE>
+__global__ void __launch_bounds__(FP_BX * FP_BY)
+cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, float *__restrict__ out,
+               const float *__restrict__ b, const float *__restrict__ rowsum, float eps,
+               double *__restrict__ norms) {
+    const int p = blockIdx.x * FP_BX + threadIdx.x;
+    const int x = blockIdx.y * FP_BY + threadIdx.y;
+    const int v = blockIdx.z;
+    const bool active = p < g.np && x < g.nx;
+    const int nmax = g.nt * g.ns * g.nz - 1;
+    const long long o = ((long long)v * g.nx + x) * g.np + p;
+    double r2 = 0.0, b2 = 0.0;
+    if (active) {
+        RayWalk w;
+        const bool hit = ray_setup(g, v, p, x, w);
+        if (MODE == 2) {
+            r2 = hit ? (double)w.nseg : 0.0;
+        } else {
+            const float val = hit ? ray_integral(w, vol, nmax) : 0.0f;
+            if (MODE == 0) {
+                out[o] = val;
+            } else {
+                const float bb = b[o];
+                const float r = bb - val;
+                const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
+                out[o] = r * sc;
+                r2 = (double)r * r;
+                b2 = (double)bb * bb;
+            }
+        }
+    }
+    if (MODE == 1) {
+        block_sum_atomic<FP_BX * FP_BY / 32>(r2, norms);
+        block_sum_atomic<FP_BX * FP_BY / 32>(b2, norms + 1);
+    } else if (MODE == 2) {
+        block_sum_atomic<FP_BX * FP_BY / 32>(r2, norms);
+    }
+}
+
+}  // namespace
+
+int cone_fp_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
+                   float eps, double *norms, int mode, cudaStream_t st) {
+    dim3 block(FP_BX, FP_BY);
+    dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, g.nb);
+    CT_REQUIRE(g.nb <= 65535, "cone_fp: at most 65535 views per launch");
+    if (mode == 0)
+        cone_fp_kernel<0><<<grid, block, 0, st>>>(g, vol, out, nullptr, nullptr, 0.0f, nullptr);
+    else if (mode == 1)
+        cone_fp_kernel<1><<<grid, block, 0, st>>>(g, vol, out, b, rowsum, eps, norms);
+    else
+        cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, 0.0f, norms);
+    CT_LAUNCH_CHECK("cone_fp_kernel");
+    return CT_OK;
+}
+
+}  // namespace ct

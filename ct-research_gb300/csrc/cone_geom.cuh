@@ -1,0 +1,25 @@
+// cone_geom.cuh -- cone-beam geometry shared by the cone kernels.
+#pragma once
+#include "ct_common.cuh"
+
+namespace ct {
+
+// Geometry of one cone scan in the reference's conventions
+// (ProjectionCone_3D.cpp:5-22, Backprojection3D.cu:20-27).
+struct ConeGeom {
+    int nt, ns, nz;          // volume size (t fastest)
+    int nb, np, nx;          // views, detector columns (P), detector rows (xi)
+    double size[3];          // volume extent in mm
+    double res[3];           // voxel pitch Size/length
+    double D;                // source to rotation centre
+    const double2 *trig;     // per view (sin beta, cos beta), float-overload values widened
+    const float *P;          // detector column coordinates
+    const float *xi;         // detector row coordinates
+    // detector sampling as the reference derives it (Backprojection3D.cu:304-311)
+    float pint, xint, bint;  // |P1-P0|, |xi1-xi0|, |beta1-beta0|
+    float minp, maxp, minx, maxx;
+    float p0, x0;            // P[0], xi[0]
+    float psgn, xsgn;        // +1 for ascending domains, -1 for descending
+};
+
+}  // namespace ct

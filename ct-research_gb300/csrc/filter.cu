@@ -1,0 +1,113 @@
+// filter.cu -- pre-weight + Shepp-Logan-form ramp filtering of detector rows.
+//
+// out[p] = dP * sum_q in'[q] * G[(np-1) + p - q], G the taps of GFunction
+// (FDK.cu:6-19): G[np-1] = 1/(pi dP)^2, G[np-1 +- n] = -1/(pi dP)^2/(4n^2-1).
+// in' is the row after the cosine pre-weight w (FDK: D/sqrt(D^2+P^2+xi^2),
+// FDK.cu:34; FBPfan: R/sqrt(R^2+P^2), FBPfan.cu:32; FBPparallel: none).
+//
+// The reference applies w in place inside the same kernel that convolves the
+// row, one P-tile (256 samples for FDK, 128 for FBPfan) per launch and
+// `limit` taps per launch chunk (FDK.cu:333-477).  LAUNCH_ORDER mode models
+// what that produces on a GPU: the outputs of a P-tile see the tiles launched
+// before it fully weighted, their own tile weighted once per chunk processed
+// so far, and later tiles unweighted; rows of the residual row tile launch
+// the residual P-tile first.  CLEAN mode weights the whole row once.
+//
+// One block per row; the row, its mixed copy and the taps live in shared
+// memory.  Partial sums run in FP32 and are flushed into a double every 128
+// taps; each chunk result is added into the float output as the reference's
+// `dev_Rcov[...] += PInt * Rcovsum` does.
+#include "kernels.cuh"
+
+namespace ct {
+
+
+namespace {
+
+constexpr int FT = 256;
+
+__global__ void __launch_bounds__(FT)
+row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restrict__ out) {
+    extern __shared__ float sm[];
+    const int np = f.np;
+    float *raw = sm;
+    float *mix = sm + np;
+    float *G = sm + 2 * np;
+    const int row = blockIdx.x;
+    const float *in = R + (long long)row * np;
+    float *o = out + (long long)row * np;
+    const double *w = f.w ? f.w + (long long)(row % f.wrows) * np : nullptr;
+    for (int q = threadIdx.x; q < np; q += blockDim.x) {
+        raw[q] = in[q];
+        o[q] = 0.0f;
+    }
+    for (int q = threadIdx.x; q < 2 * np - 1; q += blockDim.x) G[q] = f.G[q];
+    __syncthreads();
+
+    const int gtime = (np + f.limit - 1) / f.limit;
+    const int nfull = np / f.tile, resid = np % f.tile;
+    const int ntiles = nfull + (resid ? 1 : 0);
+    const bool launch_order = f.launch_order && w;
+    // launch position of each P-tile for this row
+    const int ridx = row % f.rowmod;
+    const bool resid_rows = (f.rowmod % f.row_block) != 0 && ridx >= (f.rowmod / f.row_block) * f.row_block;
+    auto pos_of = [&](int k) { return (resid_rows && resid) ? (k == nfull ? 0 : k + 1) : k; };
+
+    const int nsteps = launch_order ? ntiles : 1;
+    for (int step = 0; step < nsteps; ++step) {
+        int k = 0, p0 = 0, p1 = np;
+        if (launch_order) {
+            for (int j = 0; j < ntiles; ++j)
+                if (pos_of(j) == step) k = j;
+            p0 = k * f.tile;
+            p1 = (k == nfull) ? np : p0 + f.tile;
+        }
+        for (int c = 0; c < gtime; ++c) {
+            const int g0 = c * f.limit, g1 = (c == gtime - 1) ? np : (c + 1) * f.limit;
+            // the row as this chunk's launch reads it
+            for (int q = g0 + threadIdx.x; q < g1; q += blockDim.x) {
+                float v = raw[q];
+                if (w) {
+                    int e = 1;
+                    if (launch_order) {
+                        const int j = q / f.tile;
+                        const int pj = pos_of(j);
+                        e = (pj < step) ? gtime : (j == k ? c + 1 : 0);
+                    }
+                    for (int i = 0; i < e; ++i) v = (float)((double)v * w[q]);
+                }
+                mix[q] = v;
+            }
+            __syncthreads();
+            for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+                double dacc = 0.0;
+                float acc = 0.0f;
+                const float *gp = G + (np - 1) + p;
+                int n = 0;
+                for (int q = g0; q < g1; ++q) {
+                    acc = fmaf(mix[q], gp[-q], acc);
+                    if (++n == 128) { dacc += acc; acc = 0.0f; n = 0; }
+                }
+                dacc += acc;
+                o[p] = (float)((double)o[p] + (double)f.pint * dacc);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace
+
+int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st) {
+    CT_REQUIRE(f.np >= 2, "row filter: at least 2 detector samples");
+    const size_t smem = sizeof(float) * (size_t)(4 * f.np - 1);
+    CT_REQUIRE(smem <= 200 * 1024, "row filter: detector row too long for shared memory");
+    if (smem > 48 * 1024)
+        CT_CUDA(cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                "row_filter smem attribute");
+    row_filter_kernel<<<f.nrow, FT, smem, st>>>(f, R, out);
+    CT_LAUNCH_CHECK("row_filter_kernel");
+    return CT_OK;
+}
+
+}  // namespace ct

@@ -1,0 +1,50 @@
+// kernels.cuh -- kernel launchers of libctgb and the geometry they take.
+#pragma once
+#include "cone_geom.cuh"
+
+namespace ct {
+
+// 2D fan / parallel geometry (ProjectionFan_2D.cpp, BackprojectionFan2D.cpp,
+// FBPfan.cpp, ProjectionParallel_2D.cpp, FBPparallel.cpp argument sets).
+struct FanGeom {
+    int nt, ns;              // image size (t fastest)
+    int nb, np;              // views, detector bins
+    double size[2];          // image extent in mm along t and s
+    double res[2];           // pixel pitch
+    double D;                // source to centre (Rscan); unused for parallel beam
+    const double2 *trig_d;   // per view (sin, cos) of the double angles (forward projectors)
+    const double *Pd;        // double detector coordinates (forward projectors)
+    const float2 *trig_f;    // per view (sinf, cosf) of the float angles (backprojectors)
+    const float *Pf;         // float detector coordinates (backprojectors)
+    float pint, bint, minp, maxp, p0, psgn;
+    int parallel;            // 1: parallel-beam geometry
+    double smax;             // parallel: max |t| (ProjectionParallel_2D.cu:25)
+};
+
+// Detector-row filter job (filter.cu).
+struct RowFilter {
+    int nrow, np;
+    float pint;
+    const float *G;          // 2*np-1 taps
+    const double *w;         // pre-weight table [wrows][np], or nullptr
+    int wrows;               // weight row = row % wrows
+    int launch_order;        // 0 clean, 1 reference launch order
+    int tile, limit, row_block, rowmod;   // reference tiling
+};
+
+int cone_fp_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
+                   float eps, double *norms, int mode, cudaStream_t st);
+size_t cone_quads_bytes(const ConeGeom &g);
+int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, cudaStream_t st);
+int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting, const float *colsum,
+                   float eps, float lambda, float lo, float hi, bool update, cudaStream_t st);
+int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st);
+int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
+                  float eps, double *norms, int mode, cudaStream_t st);
+int fan_bp_launch(const FanGeom &g, const float *R, float *img, int wmode, const float *colsum, float eps,
+                  float lambda, float lo, float hi, bool update, cudaStream_t st);
+int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int nz, int iters, float step,
+                   float eps, float lo, cudaStream_t st);
+int sq_diff_sum_launch(const float *a, const float *b, long long n, double *out, cudaStream_t st);
+
+}  // namespace ct

@@ -1,0 +1,82 @@
+"""Build libctgb.so (the sm_103a kernels + C ABI) in-tree with nvcc.
+
+Each .cu file compiles in parallel to an object, then one link step makes
+``ctgb/_lib/libctgb.so``.  Only ``-gencode arch=compute_103a,code=sm_103a``
+is generated: the library is for GB300 only.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent                      # ct-research_gb300/
+REPO = ROOT.parent
+CSRC = ROOT / "csrc"
+INCLUDE = REPO / "include"
+LIBDIR = PKG / "_lib"
+LIB = LIBDIR / "libctgb.so"
+OBJDIR = LIBDIR / "obj"
+
+SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA 13 toolkit is required to build libctgb")
+    return exe
+
+
+def _flags(extra: list[str] | None = None) -> list[str]:
+    return ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-O2", f"-I{INCLUDE}", f"-I{CSRC}",
+            "--expt-relaxed-constexpr", *(extra or [])]
+
+
+def _stale() -> bool:
+    if not LIB.exists():
+        return True
+    t = LIB.stat().st_mtime
+    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + [INCLUDE / "ctgb.h", Path(__file__)]
+    return any(p.stat().st_mtime > t for p in deps if p.exists())
+
+
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> Path:
+    """Compile the library if any source is newer than it; returns its path."""
+    if not force and not ptxas_info and not _stale():
+        return LIB
+    OBJDIR.mkdir(parents=True, exist_ok=True)
+    exe = nvcc()
+    extra = ["-Xptxas", "-v"] if ptxas_info else []
+
+    def one(src: str):
+        obj = OBJDIR / (Path(src).stem + ".o")
+        cmd = [exe, *_flags(extra), "-c", str(CSRC / src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
+        return obj, r.stderr
+
+    jobs = min(len(SOURCES), os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        results = list(ex.map(one, SOURCES))
+    if verbose or ptxas_info:
+        for _, err in results:
+            if err:
+                print(err)
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [exe, *ARCH, "-shared", "-o", str(tmp), *[str(o) for o, _ in results], "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="--force" in sys.argv, verbose=True, ptxas_info="--ptxas" in sys.argv))

@@ -1,0 +1,184 @@
+"""Device-resident operators on torch CUDA tensors (plans over libctgb).
+
+A plan uploads the scan geometry once; its methods take and return float32
+CUDA tensors in the reference layouts and queue work on the current torch
+stream.  This is the path the SIRT loops use: data never leaves HBM.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import ConeGeometry, FanGeometry
+
+FDK_FILTER_CLEAN, FDK_FILTER_LAUNCH_ORDER = 0, 1
+FDK_BP_ZERO, FDK_BP_STICKY = 0, 1
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _tptr(t: torch.Tensor):
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if t.dtype not in (torch.float32, torch.float64):
+        raise ValueError("expected float32 (or float64 scratch) tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class ConePlan:
+    """Cone-beam operators for one ConeGeometry (ct_cone_plan_*)."""
+
+    def __init__(self, geom: ConeGeometry, fdk_filter: int = FDK_FILTER_LAUNCH_ORDER, fdk_bp: int = FDK_BP_STICKY):
+        self.geom = geom
+        self._h = C.c_void_p()
+        size = np.asarray(geom.size, np.float64)
+        self._keep = (size, geom.beta, geom.P, geom.xi)
+        _lib.call("ct_cone_plan_create", C.byref(self._h), geom.nt, geom.ns, geom.nz, _np_ptr(size),
+                  _np_ptr(geom.beta), len(geom.beta), _np_ptr(geom.P), len(geom.P), _np_ptr(geom.xi),
+                  len(geom.xi), float(geom.D))
+        _lib.call("ct_cone_plan_set_fdk_mode", self._h, int(fdk_filter), int(fdk_bp))
+        self._norms = None
+
+    def close(self):
+        if self._h:
+            _lib.lib().ct_cone_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def new_volume(self, device="cuda"):
+        return torch.zeros(self.geom.vol_shape, dtype=torch.float32, device=device)
+
+    def new_sino(self, device="cuda"):
+        return torch.zeros(self.geom.sino_shape, dtype=torch.float32, device=device)
+
+    def fp(self, vol: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        out = self.new_sino(vol.device) if out is None else out
+        _lib.call("ct_cone_fp", self._h, _tptr(vol), _tptr(out), _stream())
+        return out
+
+    def fp_residual(self, vol, b, rowsum=None, eps=0.0, out=None, norms=None):
+        """out = (b - A vol) / (rowsum + eps); norms (float64[2]) += (|b - A vol|^2, |b|^2)."""
+        out = torch.empty_like(b) if out is None else out
+        if norms is None:
+            norms = torch.zeros(2, dtype=torch.float64, device=vol.device)
+        _lib.call("ct_cone_fp_residual", self._h, _tptr(vol), _tptr(b), _tptr(rowsum), float(eps), _tptr(out),
+                  _tptr(norms), _stream())
+        return out, norms
+
+    def bp(self, proj: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        out = self.new_volume(proj.device) if out is None else out
+        _lib.call("ct_cone_bp", self._h, _tptr(proj), _tptr(out), _stream())
+        return out
+
+    def bp_update(self, proj, colsum, vol, lam=1.0, eps=0.0, lo=0.0, hi=float("inf")):
+        """vol = clamp(vol + lam * BP(proj) / (colsum + eps), lo, hi), in place."""
+        _lib.call("ct_cone_bp_update", self._h, _tptr(proj), _tptr(colsum), float(eps), float(lam), float(lo),
+                  float(hi), _tptr(vol), _stream())
+        return vol
+
+    def fdk(self, proj: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        out = self.new_volume(proj.device) if out is None else out
+        _lib.call("ct_cone_fdk", self._h, _tptr(proj), _tptr(out), _stream())
+        return out
+
+    def count_segments(self) -> int:
+        n = C.c_longlong()
+        _lib.call("ct_cone_count_segments", self._h, C.byref(n), _stream())
+        return int(n.value)
+
+    def workspace_bytes(self) -> int:
+        return int(_lib.lib().ct_cone_plan_workspace_bytes(self._h))
+
+
+class FanPlan:
+    """2D fan-beam operators for one FanGeometry (ct_fan_plan_*)."""
+
+    def __init__(self, geom: FanGeometry):
+        self.geom = geom
+        self._h = C.c_void_p()
+        size = np.asarray(geom.size, np.float64)
+        self._keep = (size, geom.beta, geom.P)
+        _lib.call("ct_fan_plan_create", C.byref(self._h), geom.nt, geom.ns, _np_ptr(size), _np_ptr(geom.beta),
+                  len(geom.beta), _np_ptr(geom.P), len(geom.P), float(geom.D))
+
+    def close(self):
+        if self._h:
+            _lib.lib().ct_fan_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def new_image(self, device="cuda"):
+        return torch.zeros(self.geom.img_shape, dtype=torch.float32, device=device)
+
+    def new_sino(self, device="cuda"):
+        return torch.zeros(self.geom.sino_shape, dtype=torch.float32, device=device)
+
+    def fp(self, img, out=None):
+        out = self.new_sino(img.device) if out is None else out
+        _lib.call("ct_fan_fp", self._h, _tptr(img), _tptr(out), _stream())
+        return out
+
+    def fp_residual(self, img, b, rowsum=None, eps=0.0, out=None, norms=None):
+        out = torch.empty_like(b) if out is None else out
+        if norms is None:
+            norms = torch.zeros(2, dtype=torch.float64, device=img.device)
+        _lib.call("ct_fan_fp_residual", self._h, _tptr(img), _tptr(b), _tptr(rowsum), float(eps), _tptr(out),
+                  _tptr(norms), _stream())
+        return out, norms
+
+    def bp(self, proj, out=None):
+        out = self.new_image(proj.device) if out is None else out
+        _lib.call("ct_fan_bp", self._h, _tptr(proj), _tptr(out), _stream())
+        return out
+
+    def bp_update(self, proj, colsum, img, lam=1.0, eps=0.0, lo=0.0, hi=float("inf")):
+        _lib.call("ct_fan_bp_update", self._h, _tptr(proj), _tptr(colsum), float(eps), float(lam), float(lo),
+                  float(hi), _tptr(img), _stream())
+        return img
+
+    def fbp(self, proj, out=None, filter_mode=FDK_FILTER_LAUNCH_ORDER):
+        out = self.new_image(proj.device) if out is None else out
+        _lib.call("ct_fan_fbp", self._h, _tptr(proj), _tptr(out), int(filter_mode), _stream())
+        return out
+
+
+def tv_flow(x: torch.Tensor, iters: int, step: float, eps: float = 1e-8, lo: float = 0.0, work=None, scratch=None):
+    """Normalised isotropic TV gradient-flow sub-iterations on x ([nz][ny][nx] or [ny][nx]), in place."""
+    if x.dim() == 2:
+        nz, (ny, nx) = 1, x.shape
+    else:
+        nz, ny, nx = x.shape
+    work = torch.empty_like(x) if work is None else work
+    scratch = torch.zeros(2, dtype=torch.float64, device=x.device) if scratch is None else scratch
+    _lib.call("ct_tv_flow", _tptr(x), _tptr(work), _tptr(scratch), nx, ny, nz, int(iters), float(step), float(eps),
+              float(lo), _stream())
+    return x
+
+
+def sq_diff_sum(a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    out = torch.zeros(1, dtype=torch.float64, device=a.device) if out is None else out
+    _lib.call("ct_sq_diff_sum", _tptr(a), _tptr(b), int(a.numel()), _tptr(out), _stream())
+    return out

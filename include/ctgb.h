@@ -1,0 +1,182 @@
+/*
+ * ctgb.h -- C ABI of the GB300 (sm_103a) CT projector / backprojector library
+ * (libctgb.so).  A drop-in for the host helpers behind the CT-Research MEX
+ * operators, plus device-pointer entry points for reconstruction loops that
+ * keep all data in HBM.
+ *
+ * Conventions (identical to the reference operators):
+ *   volume     float [z][s][t], t fastest      (ProjectionCone_3D.cu:366)
+ *   cone sino  float [beta][xi][P], P fastest  (ProjectionCone_3D.cu:16)
+ *   2D image   float [s][t], t fastest         (ProjectionFan_2D.cu:207)
+ *   2D sino    [beta][P], P fastest            (ProjectionFan_2D.cu:15)
+ *   angles in radians; world coordinates run 0..Size (mm), rotation centre
+ *   Size/2; the source sits at (C_t - D sin(beta), C_s + D cos(beta), C_z);
+ *   P and xi are coordinates on a virtual flat detector through the centre.
+ *
+ * Every entry point returns a ct_status (0 = success) instead of the
+ * reference's cudaError_t; ct_last_error() gives a message for the last
+ * failure on the calling thread.  No entry point resets the device.
+ */
+#ifndef CTGB_H
+#define CTGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CT_OK = 0,
+    CT_ERR_ARG = 1,      /* invalid size, geometry or pointer */
+    CT_ERR_OOM = 2,      /* device allocation failed */
+    CT_ERR_LAUNCH = 3,   /* kernel launch failed */
+    CT_ERR_CUDA = 4,     /* other CUDA runtime error (copy, sync, ...) */
+    CT_ERR_TIMEOUT = 5   /* a bounded device wait gave up */
+} ct_status;
+
+/* Message of the last failure on this thread ("" when none). */
+const char *ct_last_error(void);
+/* Library version string. */
+const char *ct_version(void);
+
+/* ===================================================================== */
+/* Drop-in host-pointer entry points.  Arguments, their meaning and the   */
+/* output layout are those of the reference host helpers named in each   */
+/* comment; device buffers are managed inside (cached between calls).     */
+/* ===================================================================== */
+
+/* Cone-beam Siddon forward projection.
+ * Replaces ProjectionCone_3D() (GPU_accelerated_Operator/ProjectionCone_3D/
+ * ProjectionCone_3D.h:32-35, body ProjectionCone_3D.cu:382-645).
+ * resolution = {Size_t/t_length, Size_s/s_length, Size_z/z_length}. */
+int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaScanRange,
+                         const float *Pdomain, const float *Xigamadomain, int t_length, int s_length,
+                         int z_length, double Center_t, double Center_s, double Center_z, int LBeta,
+                         int LP, int LXigama, double Distance, const double *resolution);
+
+/* Cone-beam voxel-driven backprojection with chord weight (the A^T of the
+ * cone iterative methods).  Replaces BackPro() (GPU_accelerated_Operator/
+ * BackprojectionCone_3D/Backprojection3D.h:31-33, body Backprojection3D.cu:294-557). */
+int ct_BackPro(float *Display, const float *R, const float *Xigamadomain, const float *Pdomain,
+               const float *BetaScanRange, double Distance, int LBeta, int LP, int LXigama,
+               const double *Size, int t_length, int s_length, int z_length);
+
+/* FDK: cosine pre-weight, Shepp-Logan ramp, weighted bilinear backprojection.
+ * Replaces FDKpro() (Analytic_Algorithm/FBP_type_analytic_algorithm_GPU_cpp_sourcecode/
+ * FDK_GPU/FDK.h:29-31, body FDK.cu:129-611).  R is not modified. */
+int ct_FDKpro(float *Display, const float *R, const float *Xigamadomain, const float *Pdomain,
+              const float *BetaScanRange, double Distance, int LBeta, int LP, int LXigama,
+              const double *Size, int t_length, int s_length, int z_length);
+
+/* 2D fan-beam Siddon forward projection (double output, double angles/bins).
+ * Replaces ProjectionFan_2D() (GPU_accelerated_Operator/ProjectionFan_2D/
+ * ProjectionFan_2D.h:32-34, body ProjectionFan_2D.cu:223-475). */
+int ct_ProjectionFan_2D(const float *Pic, double *Projection, const double *BetaScanRange,
+                        const double *Pdomain, int t_length, int s_length, double Center_t,
+                        double Center_s, int LBeta, int LP, double Distance, const double *resolution);
+
+/* 2D parallel-beam Siddon forward projection.
+ * Replaces ProjectionParallel_2D() (GPU_accelerated_Operator/ProjectionParallel_2D/
+ * ProjectionParallel_2D.h:33-35, body ProjectionParallel_2D.cu:256-483). */
+int ct_ProjectionParallel_2D(const float *Pic, double *Projection, const double *thetaRange,
+                             const double *t_Range, int height, int width, double Center_y,
+                             double Center_x, int Ltheta, int Lt, const double *resolution);
+
+/* 2D fan voxel-driven backprojection (unfiltered; the A^T of 2D SIRT).
+ * Replaces FBPfan() of GPU_accelerated_Operator/BackprojectionFan_2D
+ * (BackprojectionFan2D.h:35-36, body BackprojectionFan2D.cu:119-349). */
+int ct_BackprojectionFan2D(float *Display, const float *R, const float *Pdomain,
+                           const float *BetaScanRange, int LBeta, int LP, const double *Size,
+                           int t_length, int s_length, double Rscan);
+
+/* 2D fan FBP: pre-weight, S-L ramp, 1/U^2 weighted backprojection.
+ * Replaces FBPfan() of Analytic_Algorithm/.../FBP_fan_GPU (FBPfan.h:31-32,
+ * body FBPfan.cu:99-557).  R is not modified. */
+int ct_FBPfan(float *Display, const float *R, const float *Pdomain, const float *BetaScanRange,
+              int LBeta, int LP, const double *Size, int t_length, int s_length, double Rscan);
+
+/* 2D parallel FBP: S-L ramp and linear-interpolation backprojection.
+ * Replaces FBPpara() (Analytic_Algorithm/.../FBP_parallel_GPU/FBPparallel.h:31-32). */
+int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float *ThetaScanRange,
+               int LTheta, int LT, const double *Size, int t_length, int s_length);
+
+/* ===================================================================== */
+/* Plans and device-pointer entry points (data stays in HBM).             */
+/* ===================================================================== */
+
+typedef struct ct_cone_plan ct_cone_plan;
+typedef struct ct_fan_plan ct_fan_plan;
+
+/* Behaviour switches of the plans.  CT_COMPAT reproduces the reference
+ * exactly where it has data-dependent quirks; the default of every plan. */
+enum {
+    CT_FDK_FILTER_CLEAN = 0,       /* weight the whole row, then filter */
+    CT_FDK_FILTER_LAUNCH_ORDER = 1,/* reference: in-place weight seen in launch order (FDK.cu:36-44) */
+    CT_FDK_BP_ZERO = 0,            /* off-detector voxels add 0 */
+    CT_FDK_BP_STICKY = 1           /* reference: they re-add the last in-range value (FDK.cu:73,100-123) */
+};
+
+/* Cone geometry; arrays are host pointers copied into the plan.  Angles,
+ * P and xi domains as the reference's BetaScanRange / Pdomain / Xigamadomain
+ * (uniform spacing required by the backprojectors, as in the reference). */
+int ct_cone_plan_create(ct_cone_plan **plan, int t_length, int s_length, int z_length,
+                        const double *Size, const float *BetaScanRange, int LBeta,
+                        const float *Pdomain, int LP, const float *Xigamadomain, int LXigama,
+                        double Distance);
+int ct_cone_plan_destroy(ct_cone_plan *plan);
+/* FDK behaviour (CT_FDK_FILTER_*, CT_FDK_BP_*). Defaults: LAUNCH_ORDER, STICKY. */
+int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode);
+/* Device bytes of plan-owned workspace (packed sinogram, filter rows). */
+size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan);
+
+/* proj[beta][xi][P] = Siddon line integrals of vol.  All pointers are device
+ * pointers; work is queued on `stream` (cudaStream_t, 0 = legacy default). */
+int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stream);
+/* Forward projection fused with the SIRT residual: out = (b - A vol) * scale,
+ * with scale = 1/(rowsum + eps) when d_rowsum is non-NULL (else 1), and
+ * adds sum((b - A vol)^2) and sum(b^2) into d_norms[0..1] (double, device). */
+int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b,
+                        const float *d_rowsum, float eps, float *d_out, double *d_norms, void *stream);
+/* vol = BackPro(proj): chord-weighted voxel-driven backprojection. */
+int ct_cone_bp(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream);
+/* SIRT update fused into the backprojection:
+ * vol = clamp(vol + lambda * BackPro(proj) / (colsum + eps), lo, hi). */
+int ct_cone_bp_update(ct_cone_plan *plan, const float *d_proj, const float *d_colsum, float eps,
+                      float lambda, float lo, float hi, float *d_vol, void *stream);
+/* FDK reconstruction of d_proj into d_vol (modes from ct_cone_plan_set_fdk_mode). */
+int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream);
+/* Exact number of Siddon segments over all rays of the plan (host result). */
+int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream);
+
+/* 2D fan plan (ProjectionFan_2D / BackprojectionFan2D / FBPfan geometry). */
+int ct_fan_plan_create(ct_fan_plan **plan, int t_length, int s_length, const double *Size,
+                       const double *BetaScanRange, int LBeta, const double *Pdomain, int LP,
+                       double Distance);
+int ct_fan_plan_destroy(ct_fan_plan *plan);
+int ct_fan_fp(ct_fan_plan *plan, const float *d_img, float *d_proj, void *stream);
+int ct_fan_fp_residual(ct_fan_plan *plan, const float *d_img, const float *d_b, const float *d_rowsum,
+                       float eps, float *d_out, double *d_norms, void *stream);
+int ct_fan_bp(ct_fan_plan *plan, const float *d_proj, float *d_img, void *stream);
+int ct_fan_bp_update(ct_fan_plan *plan, const float *d_proj, const float *d_colsum, float eps,
+                     float lambda, float lo, float hi, float *d_img, void *stream);
+int ct_fan_fbp(ct_fan_plan *plan, const float *d_proj, float *d_img, int filter_mode, void *stream);
+
+/* ===================================================================== */
+/* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */
+/* ===================================================================== */
+
+/* Isotropic TV gradient-flow sub-iterations on a [nz][ny][nx] volume
+ * (nz = 1 for 2D):  x <- max(x - step * g / rms(g), lo) with g the gradient
+ * of sum sqrt(|forward-difference grad x|^2 + eps^2); `iters` steps.  d_work
+ * must hold nx*ny*nz floats; d_scratch 2 doubles. */
+int ct_tv_flow(float *d_x, float *d_work, double *d_scratch, int nx, int ny, int nz, int iters,
+               float step, float eps, float lo, void *stream);
+/* d_norm[0] += sum((a - b)^2) over n floats (double accumulation). */
+int ct_sq_diff_sum(const float *d_a, const float *d_b, long long n, double *d_norm, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTGB_H */

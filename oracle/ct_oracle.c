@@ -1,0 +1,909 @@
+/*
+ * ct_oracle.c -- FP64 CPU restatement of the CT-Research projector /
+ * backprojector operators.  TEST INFRASTRUCTURE ONLY: this file is the
+ * checker for the CUDA path (tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference arm of bench.py); nothing in the product library
+ * links or calls it.
+ *
+ * Each function follows one kernel of the reference, step for step, in the
+ * reference's own precision (double arithmetic on float data, float
+ * accumulators where the reference accumulates into float buffers), so that
+ * its output agrees with the reference kernel to the last bits on the same
+ * inputs.  The file:line of the reference code each part follows is cited.
+ * All reference paths are relative to the CT-Research project root.
+ *
+ * Build: gcc -O2 -fopenmp -ffp-contract=off -shared -fPIC (see oracle/build.py).
+ * -ffp-contract=off keeps a*b+c as two roundings on every host (x86 and Arm).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OC_API __attribute__((visibility("default")))
+
+static const double OC_EPS15 = 1e-15;   /* ProjectionCone_3D.cu:5, ProjectionFan_2D.cu:5 */
+static const double OC_ERR5 = 1e-5;     /* ProjectionParallel_2D.cu:6 */
+static const double OC_EPS30 = 1e-30;   /* ProjectionParallel_2D.cu:5 */
+static const double OC_PI = 3.141592653589793;  /* FDK.cu:4 */
+
+static inline double sq(double x) { return 1.0 * x * x; }
+static inline double slope_clamp(double x) {   /* Maxlim / Minlim, ProjectionCone_3D.h:29-30 */
+    x = x > 1e16 ? 1e16 : x;
+    return x < -1e16 ? -1e16 : x;
+}
+static inline double dist3sq(double a0, double a1, double a2, double b0, double b1, double b2) {
+    return sq(a0 - b0) + sq(a1 - b1) + sq(a2 - b2);
+}
+static inline double dist2sq(double a0, double a1, double b0, double b1) {
+    return sq(a0 - b0) + sq(a1 - b1);
+}
+static void set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3D cone-beam Siddon forward projection: one ray (beta, P, xi).           */
+/* Follows ProjectionCone (ProjectionCone_3D.cu:8-379).                    */
+/* ------------------------------------------------------------------------ */
+static float cone_ray(const float *vol, int nt, int ns, int nz, const double res[3],
+                      double ct, double cs, double cz, float beta, float P, float xi, double D)
+{
+    const double r1 = res[0], r2 = res[1], r3 = res[2];
+    /* source and far end of the ray, :26-42 */
+    /* Beta is a float kernel argument, so sin(Beta)/cos(Beta) resolve to the
+       single-precision overloads in the reference (C++ overloading). */
+    const double sb = sinf(beta), cb = cosf(beta);
+    double src_t = ct - D * sb;
+    double src_s = cs + D * cb;
+    double src_z = cz;
+    double gama = atan(xi / D);
+    double dshift = D / cos(gama);
+    double theta = atan(P / dshift);
+    double smax = 2 * D;
+    double end_t = ct + smax * sin(theta) * cb - (D - smax * cos(theta) * cos(gama)) * sb;
+    double end_s = cs + smax * sin(theta) * sb + (D - smax * cos(theta) * cos(gama)) * cb;
+    double end_z = cz + smax * cos(theta) * sin(gama);
+
+    /* six slopes, :44-84 */
+    double dt = end_t - src_t, ds = end_s - src_s, dz = end_z - src_z;
+    double t2s, t2z, s2t, s2z, z2t, z2s;
+    if (dt == 0) { t2s = ds / (dt + OC_EPS15); t2z = dz / (dt + OC_EPS15); }
+    else { t2s = ds / dt; t2z = dz / dt; }
+    if (ds == 0) { s2t = dt / (ds + OC_EPS15); s2z = dz / (ds + OC_EPS15); }
+    else { s2t = dt / ds; s2z = dz / ds; }
+    if (dz == 0) { z2t = dt / (dz + OC_EPS15); z2s = ds / (dz + OC_EPS15); }
+    else { z2t = dt / dz; z2s = ds / dz; }
+    t2s = slope_clamp(t2s); t2z = slope_clamp(t2z); s2t = slope_clamp(s2t);
+    s2z = slope_clamp(s2z); z2t = slope_clamp(z2t); z2s = slope_clamp(z2s);
+
+    int sig_t = end_t >= src_t ? 1 : -1;   /* :87-108 */
+    int sig_s = end_s >= src_s ? 1 : -1;
+    int sig_z = end_z >= src_z ? 1 : -1;
+
+    /* box faces and their hit points, :111-129 */
+    double tlo = 0, thi = nt * r1, slo = 0, shi = ns * r2, zlo = 0, zhi = nz * r3;
+    double tlo_s = src_s + (tlo - src_t) * t2s, tlo_z = src_z + (tlo - src_t) * t2z;
+    double thi_s = src_s + (thi - src_t) * t2s, thi_z = src_z + (thi - src_t) * t2z;
+    double slo_t = src_t + (slo - src_s) * s2t, slo_z = src_z + (slo - src_s) * s2z;
+    double shi_t = src_t + (shi - src_s) * s2t, shi_z = src_z + (shi - src_s) * s2z;
+    double zlo_t = src_t + (zlo - src_z) * z2t, zlo_s = src_s + (zlo - src_z) * z2s;
+    double zhi_t = src_t + (zhi - src_z) * z2t, zhi_s = src_s + (zhi - src_z) * z2s;
+
+    /* first two faces found, in the reference's search order, :132-218 */
+    int f_tlo = tlo_s >= 0 && tlo_s <= shi && tlo_z >= 0 && tlo_z <= zhi;
+    int f_thi = thi_s >= 0 && thi_s <= shi && thi_z >= 0 && thi_z <= zhi;
+    int f_slo = slo_t >= 0 && slo_t <= thi && slo_z >= 0 && slo_z <= zhi;
+    int f_shi = shi_t >= 0 && shi_t <= thi && shi_z >= 0 && shi_z <= zhi;
+    int f_zlo = zlo_t >= 0 && zlo_t <= thi && zlo_s >= 0 && zlo_s <= shi;
+    int f_zhi = zhi_t >= 0 && zhi_t <= thi && zhi_s >= 0 && zhi_s <= shi;
+    double ft[6] = {tlo, thi, slo_t, shi_t, zlo_t, zhi_t};
+    double fs[6] = {tlo_s, thi_s, slo, shi, zlo_s, zhi_s};
+    double fz[6] = {tlo_z, thi_z, slo_z, shi_z, zlo, zhi};
+    int ok[6] = {f_tlo, f_thi, f_slo, f_shi, f_zlo, f_zhi};
+    int first = -1, second = -1;
+    for (int f = 0; f < 6; ++f) if (ok[f]) { first = f; break; }
+    if (first < 0 || first == 5) return 0.0f;         /* zhi alone is never a first face, :214-218 */
+    for (int f = first + 1; f < 6; ++f) if (ok[f]) { second = f; break; }
+    double T1 = ft[first], S1 = fs[first], Z1 = fz[first];
+    double T2 = 0, S2 = 0, Z2 = 0;                    /* unset second point stays 0, :132 */
+    if (second >= 0) { T2 = ft[second]; S2 = fs[second]; Z2 = fz[second]; }
+
+    /* start point = the one nearer the source, :221-233 */
+    double Ts, Ss, Zs;
+    if (dist3sq(T1, S1, Z1, src_t, src_s, src_z) >= dist3sq(T2, S2, Z2, src_t, src_s, src_z)) {
+        Ts = T2; Ss = S2; Zs = Z2;
+    } else {
+        Ts = T1; Ss = S1; Zs = Z1;
+    }
+
+    /* grid walk, :257-375 */
+    double ray = 0;
+    double tc = Ts / r1, sc = Ss / r2, zc = Zs / r3;
+    int nit = nt + ns + nz - 2;
+    int up_t = (1 + sig_t) / 2, up_s = (1 + sig_s) / 2, up_z = (1 + sig_z) / 2;
+    for (int i = 0; i < nit; ++i) {
+        short gt, gs, gz;
+        if (tc - (double)((short)tc) < OC_EPS15) gt = (short)(tc + sig_t);
+        else gt = (short)(floor(tc) + up_t);
+        double gt_s = (src_s + (gt * r1 - src_t) * t2s) / r2;
+        double gt_z = (src_z + (gt * r1 - src_t) * t2z) / r3;
+        if (sc - (double)((short)sc) < OC_EPS15) gs = (short)(sc + sig_s);
+        else gs = (short)(floor(sc) + up_s);
+        double gs_t = (src_t + (gs * r2 - src_s) * s2t) / r1;
+        double gs_z = (src_z + (gs * r2 - src_s) * s2z) / r3;
+        if (zc - (double)((short)zc) < OC_EPS15) gz = (short)(zc + sig_z);
+        else gz = (short)(floor(zc) + up_z);
+        double gz_t = (src_t + (gz * r3 - src_z) * z2t) / r1;
+        double gz_s = (src_s + (gz * r3 - src_z) * z2s) / r2;
+
+        double nt_, ns_, nz_;   /* chosen crossing point in grid units */
+        double dT = dist3sq(gt, gt_s, gt_z, tc, sc, zc);
+        double dS = dist3sq(gs_t, gs, gs_z, tc, sc, zc);
+        double dZ = dist3sq(gz_t, gz_s, gz, tc, sc, zc);
+        if (dT <= dS) {
+            if (dZ <= dT) { nt_ = gz_t; ns_ = gz_s; nz_ = gz; }
+            else { nt_ = gt; ns_ = gt_s; nz_ = gt_z; }
+        } else {
+            if (dZ <= dS) { nt_ = gz_t; ns_ = gz_s; nz_ = gz; }
+            else { nt_ = gs_t; ns_ = gs; nz_ = gs_z; }
+        }
+        double w = sqrt(dist3sq(nt_ * r1, ns_ * r2, nz_ * r3, tc * r1, sc * r2, zc * r3));
+        short it = (short)floor((nt_ + tc) / 2);
+        short is = (short)floor((ns_ + sc) / 2);
+        short iz = (short)floor((nz_ + zc) / 2);
+        tc = nt_; sc = ns_; zc = nz_;
+        if (it >= 0 && it < nt && is >= 0 && is < ns && iz >= 0 && iz < nz) {
+            long id = (long)iz * nt * ns + (long)is * nt + it;
+            ray += w * vol[id];
+        } else {
+            break;
+        }
+    }
+    return (float)ray;
+}
+
+OC_API void oc_cone_fp(const float *vol, float *proj, const float *beta, const float *P,
+                       const float *xi, int nt, int ns, int nz, double ct, double cs, double cz,
+                       int nb, int np, int nx, double D, const double *res, int nthreads)
+{
+    set_threads(nthreads);
+    long nray = (long)nb * nx * np;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (long r = 0; r < nray; ++r) {
+        int ip = (int)(r % np);
+        int ix = (int)((r / np) % nx);
+        int ib = (int)(r / ((long)np * nx));
+        proj[r] = cone_ray(vol, nt, ns, nz, res, ct, cs, cz, beta[ib], P[ip], xi[ix], D);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shared detector-range bookkeeping of the voxel-driven backprojectors.    */
+/* PInt/XigamaInt/minP/maxP are computed in float as in BackPro            */
+/* (Backprojection3D.cu:304-311) and FDKpro (FDK.cu:140-147).              */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    float pint, xint, bint, minp, maxp, minx, maxx;
+} det_range;
+
+static det_range make_range(const float *P, int np, const float *xi, int nx, const float *beta, int nb)
+{
+    det_range r;
+    r.pint = fabsf(P[1] - P[0]);
+    r.xint = (xi && nx > 1) ? fabsf(xi[1] - xi[0]) : 0.0f;
+    r.bint = (beta && nb > 1) ? fabsf(beta[1] - beta[0]) : 0.0f;
+    r.maxp = P[0] > P[np - 1] ? P[0] : P[np - 1];
+    r.minp = P[0] < P[np - 1] ? P[0] : P[np - 1];
+    if (xi) {
+        r.maxx = xi[0] > xi[nx - 1] ? xi[0] : xi[nx - 1];
+        r.minx = xi[0] < xi[nx - 1] ? xi[0] : xi[nx - 1];
+    } else {
+        r.maxx = r.minx = 0;
+    }
+    return r;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3D cone voxel-driven backprojection with chord weight.                   */
+/* Follows BackProjection3D (Backprojection3D.cu:8-291); the view loop is   */
+/* the per-view launch loop of BackPro (:445-520), so the float             */
+/* accumulation order over views is the reference's.                        */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_cone_bp(float *disp, const float *R, const float *xi, const float *P,
+                       const float *beta, double D, int nb, int np, int nx, const double *size,
+                       int nt, int ns, int nz, int nthreads)
+{
+    set_threads(nthreads);
+    det_range g = make_range(P, np, xi, nx, beta, nb);
+    const double rt = 1.0 * size[0] / nt, rs = 1.0 * size[1] / ns, rz = 1.0 * size[2] / nz;
+    const double ct = size[0] / 2, cs = size[1] / 2, cz = size[2] / 2;
+    memset(disp, 0, sizeof(float) * (size_t)nt * ns * nz);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int si = 0; si < ns; ++si)
+    for (int ti = 0; ti < nt; ++ti) {
+        for (int b = 0; b < nb; ++b) {
+            const float bet = beta[b];
+            double it = (ti + 0.5) * rt - ct;
+            double is = (si + 0.5) * rs - cs;
+            const double sb = sinf(bet), cb = cosf(bet);   /* float overloads, as in the reference */
+            double dect_t = it * cb + is * sb;
+            double dect_s = -it * sb + is * cb;
+            double lr = D / (D - dect_s);
+            double p = dect_t * lr;
+            double src_t = ct - D * sb, src_s = cs + D * cb;
+            double end_t = it + ct, end_s = is + cs;
+            double tlo = ti * rt, thi = (ti + 1) * rt, slo = si * rs, shi = (si + 1) * rs;
+            for (int zi = 0; zi < nz; ++zi) {
+                double iz = (zi + 0.5) * rz - cz;
+                double x = iz * lr;
+                if (!((p >= g.minp) && (p < g.maxp) && (x >= g.minx) && (x < g.maxx))) continue;
+                unsigned short x1 = (unsigned short)floor(fabs(x - xi[0]) / g.xint);
+                unsigned short x2 = x1 + 1;
+                unsigned short p1 = (unsigned short)floor(fabs(p - P[0]) / g.pint);
+                unsigned short p2 = p1 + 1;
+                double xg1 = fabs(x - xi[x1]), xg2 = fabs(xi[x2] - x);
+                double pg1 = fabs(p - P[p1]), pg2 = fabs(P[p2] - p);
+                long vb = (long)b * np * nx;
+                double val = (xg2 * pg2 * R[vb + (long)x1 * np + p1] + xg1 * pg2 * R[vb + (long)x2 * np + p1]
+                            + xg2 * pg1 * R[vb + (long)x1 * np + p2] + xg1 * pg1 * R[vb + (long)x2 * np + p2])
+                            / (g.pint * g.xint);
+                /* chord through the voxel: entry on a low face, :243-283 */
+                double src_z = cz, end_z = iz + cz;
+                double zlo = zi * rz, zhi = (zi + 1) * rz;
+                double tlo_s = src_s + (tlo - src_t) * (end_s - src_s) / (end_t - src_t + OC_EPS15);
+                double tlo_z = src_z + (tlo - src_t) * (end_z - src_z) / (end_t - src_t + OC_EPS15);
+                double slo_t = src_t + (slo - src_s) * (end_t - src_t) / (end_s - src_s + OC_EPS15);
+                double slo_z = src_z + (slo - src_s) * (end_z - src_z) / (end_s - src_s + OC_EPS15);
+                double zlo_t = src_t + (zlo - src_z) * (end_t - src_t) / (end_z - src_z + OC_EPS15);
+                double zlo_s = src_s + (zlo - src_z) * (end_s - src_s) / (end_z - src_z + OC_EPS15);
+                double T1, S1, Z1;
+                if (tlo_s >= slo && tlo_s <= shi && tlo_z >= zlo && tlo_z <= zhi) { T1 = tlo; S1 = tlo_s; Z1 = tlo_z; }
+                else if (slo_t >= tlo && slo_t <= thi && slo_z >= zlo && slo_z <= zhi) { T1 = slo_t; S1 = slo; Z1 = slo_z; }
+                else if (zlo_t >= tlo && zlo_t <= thi && zlo_s >= slo && zlo_s <= shi) { T1 = zlo_t; S1 = zlo_s; Z1 = zlo; }
+                else break;   /* the reference returns: the rest of this column is skipped for this view, :277-281 */
+                double len = 2 * sqrt(dist3sq(T1, S1, Z1, end_t, end_s, end_z));
+                long id = (long)zi * nt * ns + (long)si * nt + ti;
+                disp[id] = (float)((double)disp[id] + val * len);
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shepp-Logan-form ramp filter taps, GFunction (FDK.cu:6-19; identical in   */
+/* FBPfan.cu:6-19 and FBPparallel.cu:6-19).  g has 2*np-1 taps, centre np-1. */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_sl_filter(float *g, float pint, int np)
+{
+    for (int n = 0; n < np; ++n) {
+        if (n == 0) g[np - 1] = (float)(1.0 / sq(OC_PI * pint));
+        else {
+            float v = (float)(-1.0 / sq(pint * OC_PI) / (4 * sq(n) - 1));
+            g[np - 1 - n] = v;
+            g[np - 1 + n] = v;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FDK: cosine pre-weight + S-L ramp + weighted bilinear BP.                 */
+/* PreWeightFilter (FDK.cu:21-48), BackProjection (FDK.cu:50-126).          */
+/* stage outputs are exposed for the parity tests: rcov may be NULL.        */
+/* ------------------------------------------------------------------------ */
+/* The pre-weighted input R * D / sqrt(D^2 + P^2 + xi^2), double product
+   rounded to float as the in-place update of PreWeightFilter (FDK.cu:34-36). */
+OC_API void oc_fdk_weight_apply(float *out, const float *R, const float *P, const float *xi, int nb,
+                                int np, int nx, double D)
+{
+    for (long b = 0; b < nb; ++b)
+        for (int x = 0; x < nx; ++x)
+            for (int p = 0; p < np; ++p) {
+                long i = (b * nx + x) * np + p;
+                out[i] = (float)(R[i] * (D / sqrt(sq(D) + sq(P[p]) + sq(xi[x]))));
+            }
+}
+
+/* Same for FBPfan: R * Rscan / sqrt(Rscan^2 + P^2) (FBPfan.cu:31-34). */
+OC_API void oc_fbpfan_weight_apply(float *out, const float *R, const float *P, int nb, int np, double rscan)
+{
+    for (long b = 0; b < nb; ++b)
+        for (int p = 0; p < np; ++p)
+            out[b * np + p] = (float)(R[b * np + p] * (rscan / sqrt(sq(rscan) + sq(P[p]))));
+}
+
+OC_API void oc_fdk_filter(float *rcov, const float *R, const float *xi, const float *P, int nb,
+                          int np, int nx, double D, int mode, int nthreads)
+{
+    set_threads(nthreads);
+    det_range rg = make_range(P, np, xi, nx, NULL, 0);
+    float *g = (float *)malloc(sizeof(float) * (2 * np - 1));
+    oc_sl_filter(g, rg.pint, np);
+    /* the weight depends on (xi, P) only; the reference recomputes it per launch
+       in double and multiplies in double, so keep it in double here */
+    double *wd = (double *)malloc(sizeof(double) * (size_t)nx * np);
+    for (int x = 0; x < nx; ++x)
+        for (int p = 0; p < np; ++p)
+            wd[(long)x * np + p] = D / sqrt(sq(D) + sq(P[p]) + sq(xi[x]));
+    /* mode 0 ("clean"): every output sees the fully pre-weighted row.
+       mode 1 ("launch order"): the reference weights the row in place inside
+       the kernel that convolves it, one P-tile of 256 samples per launch and
+       2048 taps per chunk (FDK.cu:21-48, launch loops :333-477).  Model: a
+       P-tile sees earlier tiles fully weighted, its own tile weighted once per
+       chunk processed so far, later tiles unweighted; rows of the residual
+       xi-tile run the residual P-tile first (:375-409 before :442-474). */
+#pragma omp parallel
+    {
+        float *cur = (float *)malloc(sizeof(float) * np);
+        int ntl = np / 256 + 2;
+        int *pos = (int *)malloc(sizeof(int) * ntl);
+#pragma omp for schedule(dynamic, 4)
+        for (long row = 0; row < (long)nb * nx; ++row) {
+            int x = (int)(row % nx);
+            const float *in = R + row * np;
+            const double *w = wd + (long)x * np;
+            float *out = rcov + row * np;
+            for (int p = 0; p < np; ++p) out[p] = 0.0f;
+            const int tile = 256, limit = 2048, row_block = 256;   /* FDK.h:22-24 */
+            int gtime = (int)ceil(1.0 * np / limit);
+            if (mode == 0) {
+                for (int p = 0; p < np; ++p) cur[p] = (float)(in[p] * w[p]);
+                for (int c = 0; c < gtime; ++c) {
+                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                    for (int p = 0; p < np; ++p) {
+                        double acc = 0;
+                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                        out[p] = (float)((double)out[p] + rg.pint * acc);
+                    }
+                }
+                continue;
+            }
+            int nfull = np / tile, resid = np % tile, ntiles = nfull + (resid ? 1 : 0);
+            int in_resid_rows = (nx % row_block) != 0 && x >= (nx / row_block) * row_block;
+            for (int k = 0; k < ntiles; ++k)
+                pos[k] = (in_resid_rows && resid) ? ((k == nfull) ? 0 : k + 1) : k;
+            for (int p = 0; p < np; ++p) cur[p] = in[p];
+            for (int step = 0; step < ntiles; ++step) {
+                int k = 0;
+                for (int j = 0; j < ntiles; ++j) if (pos[j] == step) k = j;
+                int p0 = k * tile, p1 = (k == nfull) ? np : p0 + tile;
+                for (int c = 0; c < gtime; ++c) {
+                    for (int p = p0; p < p1; ++p) cur[p] = (float)(cur[p] * w[p]);
+                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                    for (int p = p0; p < p1; ++p) {
+                        double acc = 0;
+                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                        out[p] = (float)((double)out[p] + rg.pint * acc);
+                    }
+                }
+            }
+        }
+        free(cur);
+        free(pos);
+    }
+    free(wd);
+    free(g);
+}
+
+/* FDK backprojection of filtered projections (FDK.cu:50-126 with the view
+   loop :508-582).  sticky=1 keeps the reference's behaviour that a voxel
+   whose projection leaves the detector re-adds the last in-range value of its
+   column (Display_pBeta is not reset, :73 and :100-123); sticky=0 adds 0. */
+OC_API void oc_fdk_bp(float *disp, const float *rcov, const float *xi, const float *P,
+                      const float *beta, double D, int nb, int np, int nx, const double *size,
+                      int nt, int ns, int nz, int sticky, int nthreads)
+{
+    set_threads(nthreads);
+    det_range g = make_range(P, np, xi, nx, beta, nb);
+    const double rt = 1.0 * size[0] / nt, rs = 1.0 * size[1] / ns, rz = 1.0 * size[2] / nz;
+    const double ct = size[0] / 2, cs = size[1] / 2, cz = size[2] / 2;
+    memset(disp, 0, sizeof(float) * (size_t)nt * ns * nz);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int si = 0; si < ns; ++si)
+    for (int ti = 0; ti < nt; ++ti) {
+        for (int b = 0; b < nb; ++b) {
+            const float bet = beta[b];
+            double it = (ti + 0.5) * rt - ct;
+            double is = (si + 0.5) * rs - cs;
+            const double sb = sinf(bet), cb = cosf(bet);   /* float overloads, as in the reference */
+            double dect_t = it * cb + is * sb;
+            double dect_s = -it * sb + is * cb;
+            double lr = D / (D - dect_s);
+            double p = dect_t * lr;
+            double val = 0;
+            for (int zi = 0; zi < nz; ++zi) {
+                double iz = (zi + 0.5) * rz - cz;
+                double x = iz * lr;
+                if ((p >= g.minp) && (p < g.maxp) && (x >= g.minx) && (x < g.maxx)) {
+                    unsigned int x1 = (unsigned int)floor(fabs(x - xi[0]) / g.xint), x2 = x1 + 1;
+                    unsigned int p1 = (unsigned int)floor(fabs(p - P[0]) / g.pint), p2 = p1 + 1;
+                    double xg1 = fabs(x - xi[x1]), xg2 = fabs(xi[x2] - x);
+                    double pg1 = fabs(p - P[p1]), pg2 = fabs(P[p2] - p);
+                    double weight = sqrt(1 + 0 * sq(iz) / (sq(D + dect_s) + sq(dect_t)));
+                    long vb = (long)b * np * nx;
+                    val = (xg2 * pg2 * rcov[vb + (long)x1 * np + p1] + xg1 * pg2 * rcov[vb + (long)x2 * np + p1]
+                         + xg2 * pg1 * rcov[vb + (long)x1 * np + p2] + xg1 * pg1 * rcov[vb + (long)x2 * np + p2])
+                         / (g.pint * g.xint) * sq(lr) * g.bint * weight;
+                } else if (!sticky) {
+                    val = 0;
+                }
+                long id = (long)zi * nt * ns + (long)si * nt + ti;
+                disp[id] = (float)((double)disp[id] + val);
+            }
+        }
+    }
+}
+
+/* full FDK chain as FDKpro (FDK.cu:129-611) */
+OC_API void oc_fdk(float *disp, const float *R, const float *xi, const float *P, const float *beta,
+                   double D, int nb, int np, int nx, const double *size, int nt, int ns, int nz,
+                   int filter_mode, int sticky, int nthreads)
+{
+    float *rcov = (float *)malloc(sizeof(float) * (size_t)nb * np * nx);
+    oc_fdk_filter(rcov, R, xi, P, nb, np, nx, D, filter_mode, nthreads);
+    oc_fdk_bp(disp, rcov, xi, P, beta, D, nb, np, nx, size, nt, ns, nz, sticky, nthreads);
+    free(rcov);
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2D fan-beam Siddon forward projection, ProjectionFan (ProjectionFan_2D.cu:8-220). */
+/* ------------------------------------------------------------------------ */
+static double fan_ray(const float *pic, int nt, int ns, double ct, double cs, const double res[2],
+                      double P, double beta, double D)
+{
+    const double r1 = res[0], r2 = res[1];
+    double src_t = ct + D * sin(-beta);
+    double src_s = cs + D * cos(-beta);
+    double theta = atan(P / D);
+    double smax = 2 * D;
+    double end_t = ct + smax * sin(theta) * cos(-beta) + (D - smax * cos(theta)) * sin(-beta);
+    double end_s = cs - smax * sin(theta) * sin(-beta) + (D - smax * cos(theta)) * cos(-beta);
+    double dt = end_t - src_t, ds = end_s - src_s;
+    double t2s = (dt == 0) ? ds / (dt + OC_EPS15) : ds / dt;
+    double s2t = (ds == 0) ? dt / (ds + OC_EPS15) : dt / ds;
+    t2s = slope_clamp(t2s); s2t = slope_clamp(s2t);
+    int sig_t = end_t >= src_t ? 1 : -1;
+    int sig_s = end_s >= src_s ? 1 : -1;
+    double tlo = 0, thi = nt * r1, slo = 0, shi = ns * r2;
+    double tlo_s = src_s + (tlo - src_t) * t2s, thi_s = src_s + (thi - src_t) * t2s;
+    double slo_t = src_t + (slo - src_s) * s2t, shi_t = src_t + (shi - src_s) * s2t;
+    int ok[4] = {tlo_s >= 0 && tlo_s <= shi, thi_s >= 0 && thi_s <= shi,
+                 slo_t >= 0 && slo_t <= thi, shi_t >= 0 && shi_t <= thi};
+    double ft[4] = {tlo, thi, slo_t, shi_t}, fs[4] = {tlo_s, thi_s, slo, shi};
+    int first = -1, second = -1;
+    for (int f = 0; f < 4; ++f) if (ok[f]) { first = f; break; }
+    if (first < 0 || first == 3) return 0.0;   /* :117-121 (shi alone is never a first face) */
+    for (int f = first + 1; f < 4; ++f) if (ok[f]) { second = f; break; }
+    double T1 = ft[first], S1 = fs[first], T2 = 0, S2 = 0;
+    if (second >= 0) { T2 = ft[second]; S2 = fs[second]; }
+    double Ts, Ss;
+    if (dist2sq(T1, S1, src_t, src_s) >= dist2sq(T2, S2, src_t, src_s)) { Ts = T2; Ss = S2; }
+    else { Ts = T1; Ss = S1; }
+    double ray = 0;
+    double tc = Ts / r1, sc = Ss / r2;
+    int up_t = (1 + sig_t) / 2, up_s = (1 + sig_s) / 2;
+    for (int i = 0; i < nt + ns - 1; ++i) {           /* :162-216 */
+        short gt, gs;
+        if (fabs(tc - round(tc)) < OC_EPS15) gt = (short)(round(tc) + sig_t);
+        else gt = (short)(floor(tc) + up_t);
+        double gt_s = (src_s + (gt * r1 - src_t) * t2s) / r2;
+        if (fabs(sc - round(sc)) < OC_EPS15) gs = (short)(round(sc) + sig_s);
+        else gs = (short)(floor(sc) + up_s);
+        double gs_t = (src_t + (gs * r2 - src_s) * s2t) / r1;
+        double w, nt_, ns_;
+        if (dist2sq(gt, gt_s, tc, sc) <= dist2sq(gs_t, gs, tc, sc)) {
+            w = sqrt(dist2sq(gt * r1, gt_s * r2, tc * r1, sc * r2));
+            nt_ = gt; ns_ = gt_s;
+        } else {
+            w = sqrt(dist2sq(gs_t * r1, gs * r2, tc * r1, sc * r2));
+            nt_ = gs_t; ns_ = gs;
+        }
+        short it = (short)floor((nt_ + tc) / 2), is = (short)floor((ns_ + sc) / 2);
+        tc = nt_; sc = ns_;
+        if (it >= 0 && it < nt && is >= 0 && is < ns) ray += w * pic[(long)is * nt + it];
+        else break;
+    }
+    return ray;
+}
+
+OC_API void oc_fan_fp(const float *pic, double *proj, const double *beta, const double *P, int nt,
+                      int ns, double ct, double cs, int nb, int np, double D, const double *res,
+                      int nthreads)
+{
+    set_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long r = 0; r < (long)nb * np; ++r) {
+        int ip = (int)(r % np), ib = (int)(r / np);
+        proj[r] = fan_ray(pic, nt, ns, ct, cs, res, P[ip], beta[ib], D);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2D parallel-beam Siddon, ProjectionParallel (ProjectionParallel_2D.cu:9-253). */
+/* ------------------------------------------------------------------------ */
+static double par_ray(const float *pic, int h, int wd, double cy, double cx, const double res[2],
+                      double t, double theta, double smax)
+{
+    double xs = cx + t * cos(-theta) + (-smax) * sin(-theta);
+    double ys = cy - t * sin(-theta) + (-smax) * cos(-theta);
+    double xe = cx + t * cos(-theta) + smax * sin(-theta);
+    double ye = cy - t * sin(-theta) + smax * cos(-theta);
+    double x2y = (xe - xs == 0) ? (ye - ys) / (xe - xs + OC_EPS30) : (ye - ys) / (xe - xs);
+    double y2x = (ye - ys == 0) ? (xe - xs) / (ye - ys + OC_EPS30) : (xe - xs) / (ye - ys);
+    x2y = slope_clamp(x2y); y2x = slope_clamp(y2x);
+    int sig_y = (ye >= ys) ? 1 : (ye < ys ? -1 : 0);
+    int sig_x = (xe >= xs) ? 1 : (xe < xs ? -1 : 0);
+    double xlo = 0, xhi = wd * res[1], ylo = 0, yhi = h * res[0];
+    double ylo_x = xs + (ylo - ys) * y2x, yhi_x = xs + (yhi - ys) * y2x;
+    double xlo_y = ys + (xlo - xs) * x2y, xhi_y = ys + (xhi - xs) * x2y;
+    /* face search order of :77-121: ylo, yhi, xlo, xhi */
+    int ok[4] = {ylo_x >= 0 && ylo_x <= xhi, yhi_x >= 0 && yhi_x <= xhi,
+                 xlo_y >= 0 && xlo_y <= yhi, xhi_y >= 0 && xhi_y <= yhi};
+    double fx[4] = {ylo_x, yhi_x, xlo, xhi}, fy[4] = {ylo, yhi, xlo_y, xhi_y};
+    int first = -1;
+    for (int f = 0; f < 4; ++f) if (ok[f]) { first = f; break; }
+    if (first < 0 || first == 3) return 0.0;
+    /* the reference looks for the second point among: after ylo -> xlo, xhi, yhi;
+       after yhi -> xlo, xhi; after xlo -> xhi */
+    static const int order[3][3] = {{2, 3, 1}, {2, 3, -1}, {3, -1, -1}};
+    int second = -1;
+    for (int k = 0; k < 3; ++k) {
+        int f = order[first][k];
+        if (f >= 0 && ok[f]) { second = f; break; }
+    }
+    double X1 = fx[first], Y1 = fy[first], X2 = 0, Y2 = 0;
+    if (second >= 0) { X2 = fx[second]; Y2 = fy[second]; }
+    double Xs, Ys;
+    if (dist2sq(X1, Y1, xs, ys) >= dist2sq(X2, Y2, xs, ys)) { Xs = X2; Ys = Y2; }
+    else { Xs = X1; Ys = Y1; }
+    double ray = 0;
+    double xc = Xs / res[1], yc = Ys / res[0];
+    int up_x = (1 + sig_x) / 2, up_y = (1 + sig_y) / 2;
+    for (int i = 0; i < h + wd - 1; ++i) {           /* :163-243 */
+        short gx, gy;
+        if (fabs(xc - round(xc)) < OC_ERR5) gx = (short)(round(xc) + sig_x);
+        else gx = (short)(floor(xc) + up_x);
+        double gx_y = (ys + (gx * res[1] - xs) * x2y) / res[0];
+        if (fabs(yc - round(yc)) < OC_ERR5) gy = (short)(round(yc) + sig_y);
+        else gy = (short)(floor(yc) + up_y);
+        double gy_x = (xs + (gy * res[0] - ys) * y2x) / res[1];
+        double w, nx_, ny_;
+        if (dist2sq(gx, gx_y, xc, yc) >= dist2sq(gy_x, gy, xc, yc)) {
+            w = sqrt(dist2sq(gy_x * res[1], gy * res[0], xc * res[1], yc * res[0]));
+            nx_ = gy_x; ny_ = gy;
+        } else {
+            w = sqrt(dist2sq(gx * res[1], gx_y * res[0], xc * res[1], yc * res[0]));
+            nx_ = gx; ny_ = gx_y;
+        }
+        short ix = (short)floor((nx_ + xc) / 2), iy = (short)floor((ny_ + yc) / 2);
+        xc = nx_; yc = ny_;
+        if (ix >= 0 && ix < wd && iy >= 0 && iy < h) ray += w * pic[(long)iy * wd + ix];
+        else break;
+    }
+    return ray;
+}
+
+OC_API void oc_par_fp(const float *pic, double *proj, const double *theta, const double *trange,
+                      int h, int wd, double cy, double cx, int nth, int nt, const double *res,
+                      int nthreads)
+{
+    set_threads(nthreads);
+    double a = fabs(trange[0]), b = fabs(trange[nt - 1]);
+    double smax = a > b ? a : b;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long r = 0; r < (long)nth * nt; ++r) {
+        int it = (int)(r % nt), ith = (int)(r / nt);
+        proj[r] = par_ray(pic, h, wd, cy, cx, res, trange[it], theta[ith], smax);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* 2D fan voxel-driven backprojection with the reference's chord-like       */
+/* weight, BackProjection (BackprojectionFan2D.cu:7-116).                   */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_fan_bp(float *disp, const float *R, const float *P, const float *beta, int nb,
+                      int np, const double *size, int nt, int ns, double rscan, int nthreads)
+{
+    set_threads(nthreads);
+    det_range g = make_range(P, np, NULL, 0, beta, nb);
+    const double rt = 1.0 * size[0] / nt, rs = 1.0 * size[1] / ns;
+    const double ct = size[0] / 2, cs = size[1] / 2;
+    memset(disp, 0, sizeof(float) * (size_t)nt * ns);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int si = 0; si < ns; ++si)
+    for (int ti = 0; ti < nt; ++ti) {
+        for (int b = 0; b < nb; ++b) {
+            const float bet = beta[b];
+            double it = (ti + 0.5) * rt - ct, is = (si + 0.5) * rs - cs;
+            const double sb = sinf(bet), cb = cosf(bet);   /* float overloads, as in the reference */
+            double p = it * cb + is * sb;
+            double s = -it * sb + is * cb;
+            double u = (rscan - s) / rscan;
+            double pd = p / u;
+            double val = 0;
+            if ((pd >= g.minp) && (pd < g.maxp)) {
+                unsigned int p1 = (unsigned int)floor(fabs(pd - P[0]) / g.pint), p2 = p1 + 1;
+                double pg1 = fabs(pd - P[p1]), pg2 = fabs(P[p2] - pd);
+                val = (pg2 * R[(long)b * np + p1] + pg1 * R[(long)b * np + p2]) / g.pint;
+            }
+            double src_t = ct - rscan * sb, src_s = cs + rscan * cb;
+            double th = atan(pd / rscan);
+            double smax = 2 * rscan;
+            double end_t = ct + smax * sin(th) * cb - (rscan - smax * cos(th)) * sb;
+            double end_s = cs + smax * sin(th) * sb + (rscan - smax * cos(th)) * cb;
+            double dt = end_t - src_t, ds = end_s - src_s;
+            double t2s = (dt == 0) ? ds / (dt + OC_EPS15) : ds / dt;
+            double s2t = (ds == 0) ? dt / (ds + OC_EPS15) : dt / ds;
+            t2s = slope_clamp(t2s); s2t = slope_clamp(s2t);
+            double tlo = ti * rt, thi = (ti + 1) * rt, slo = si * rs, shi = (si + 1) * rs;
+            double tlo_s = src_s + (tlo - src_t) * t2s;
+            double slo_t = src_t + (slo - src_s) * s2t;
+            double T1, S1;
+            if (tlo_s >= 0 && tlo_s <= shi) { T1 = tlo; S1 = tlo_s; }       /* :95-107 */
+            else if (slo_t >= 0 && slo_t <= thi) { T1 = slo_t; S1 = slo; }
+            else continue;
+            double len = 2 * sqrt(dist2sq(T1, S1, end_t, end_s));
+            long id = (long)si * nt + ti;
+            disp[id] = (float)((double)disp[id] + val * len);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* FBPfan: weight + S-L filter + 1/U^2 weighted BP (FBPfan.cu:21-96).       */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_fbpfan_filter(float *rcov, const float *R, const float *P, int nb, int np,
+                             double rscan, int mode, int nthreads)
+{
+    set_threads(nthreads);
+    float pint = fabsf(P[1] - P[0]);
+    float *g = (float *)malloc(sizeof(float) * (2 * np - 1));
+    oc_sl_filter(g, pint, np);
+    double *w = (double *)malloc(sizeof(double) * np);
+    for (int p = 0; p < np; ++p) w[p] = rscan / sqrt(sq(rscan) + sq(P[p]));
+    const int tile = 128, limit = 1024, row_block = 128;   /* FBPfan.h:24-26 */
+#pragma omp parallel
+    {
+        float *cur = (float *)malloc(sizeof(float) * np);
+        int *pos = (int *)malloc(sizeof(int) * (np / tile + 2));
+#pragma omp for schedule(dynamic, 4)
+        for (int row = 0; row < nb; ++row) {
+            const float *in = R + (long)row * np;
+            float *out = rcov + (long)row * np;
+            for (int p = 0; p < np; ++p) out[p] = 0.0f;
+            int gtime = (int)ceil(1.0 * np / limit);
+            if (mode == 0) {
+                for (int p = 0; p < np; ++p) cur[p] = (float)(in[p] * w[p]);
+                for (int c = 0; c < gtime; ++c) {
+                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                    for (int p = 0; p < np; ++p) {
+                        double acc = 0;
+                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                        out[p] = (float)((double)out[p] + pint * acc);
+                    }
+                }
+                continue;
+            }
+            int nfull = np / tile, resid = np % tile, ntiles = nfull + (resid ? 1 : 0);
+            int in_resid_rows = (nb % row_block) != 0 && row >= (nb / row_block) * row_block;
+            for (int k = 0; k < ntiles; ++k)
+                pos[k] = (in_resid_rows && resid) ? ((k == nfull) ? 0 : k + 1) : k;
+            for (int p = 0; p < np; ++p) cur[p] = in[p];
+            for (int step = 0; step < ntiles; ++step) {
+                int k = 0;
+                for (int j = 0; j < ntiles; ++j) if (pos[j] == step) k = j;
+                int p0 = k * tile, p1 = (k == nfull) ? np : p0 + tile;
+                for (int c = 0; c < gtime; ++c) {
+                    for (int p = p0; p < p1; ++p) cur[p] = (float)(cur[p] * w[p]);
+                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                    for (int p = p0; p < p1; ++p) {
+                        double acc = 0;
+                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                        out[p] = (float)((double)out[p] + pint * acc);
+                    }
+                }
+            }
+        }
+        free(cur);
+        free(pos);
+    }
+    free(w);
+    free(g);
+}
+
+OC_API void oc_fbpfan_bp(float *disp, const float *rcov, const float *P, const float *beta, int nb,
+                         int np, const double *size, int nt, int ns, double rscan, int nthreads)
+{
+    set_threads(nthreads);
+    det_range g = make_range(P, np, NULL, 0, beta, nb);
+    const double rt = 1.0 * size[0] / nt, rs = 1.0 * size[1] / ns;
+    const double ct = size[0] / 2, cs = size[1] / 2;
+    memset(disp, 0, sizeof(float) * (size_t)nt * ns);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int si = 0; si < ns; ++si)
+    for (int ti = 0; ti < nt; ++ti) {
+        for (int b = 0; b < nb; ++b) {
+            const float bet = beta[b];
+            double it = (ti + 0.5) * rt - ct, is = (si + 0.5) * rs - cs;
+            const double sb = sinf(bet), cb = cosf(bet);   /* float overloads, as in the reference */
+            double p = it * cb + is * sb;
+            double s = -it * sb + is * cb;
+            double u = (rscan - s) / rscan;
+            double pd = p / u;
+            double val = 0;
+            if ((pd >= g.minp) && (pd < g.maxp)) {
+                unsigned int p1 = (unsigned int)floor(fabs(pd - P[0]) / g.pint), p2 = p1 + 1;
+                double pg1 = fabs(pd - P[p1]), pg2 = fabs(P[p2] - pd);
+                val = (pg2 * rcov[(long)b * np + p1] + pg1 * rcov[(long)b * np + p2]) / (sq(u) * g.pint) * g.bint;
+            }
+            long id = (long)si * nt + ti;
+            disp[id] = (float)((double)disp[id] + val);
+        }
+    }
+}
+
+OC_API void oc_fbpfan(float *disp, const float *R, const float *P, const float *beta, int nb, int np,
+                      const double *size, int nt, int ns, double rscan, int filter_mode, int nthreads)
+{
+    float *rcov = (float *)malloc(sizeof(float) * (size_t)nb * np);
+    oc_fbpfan_filter(rcov, R, P, nb, np, rscan, filter_mode, nthreads);
+    oc_fbpfan_bp(disp, rcov, P, beta, nb, np, size, nt, ns, rscan, nthreads);
+    free(rcov);
+}
+
+/* ------------------------------------------------------------------------ */
+/* FBPparallel: S-L filter (no weight) + linear-interpolation BP            */
+/* (FBPparallel.cu:21-89).                                                   */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_fbppar(float *disp, const float *R, const float *T, const float *theta, int nth,
+                      int nt_det, const double *size, int nt, int ns, int nthreads)
+{
+    set_threads(nthreads);
+    float tint = fabsf(T[1] - T[0]);
+    float thint = nth > 1 ? fabsf(theta[1] - theta[0]) : 0.0f;
+    float maxt = T[0] > T[nt_det - 1] ? T[0] : T[nt_det - 1];
+    float mint = T[0] < T[nt_det - 1] ? T[0] : T[nt_det - 1];
+    float *g = (float *)malloc(sizeof(float) * (2 * nt_det - 1));
+    oc_sl_filter(g, tint, nt_det);
+    float *rcov = (float *)malloc(sizeof(float) * (size_t)nth * nt_det);
+    const int limit = 2048;   /* FBPparallel.h:26 */
+    int gtime = (int)ceil(1.0 * nt_det / limit);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int row = 0; row < nth; ++row) {
+        const float *in = R + (long)row * nt_det;
+        float *out = rcov + (long)row * nt_det;
+        for (int p = 0; p < nt_det; ++p) out[p] = 0.0f;
+        for (int c = 0; c < gtime; ++c) {
+            int g0 = c * limit, g1 = (c == gtime - 1) ? nt_det : (c + 1) * limit;
+            for (int p = 0; p < nt_det; ++p) {
+                double acc = 0;
+                for (int q = g0; q < g1; ++q) acc += in[q] * g[(nt_det - 1) + p - q];
+                out[p] = (float)((double)out[p] + tint * acc);
+            }
+        }
+    }
+    const double rt = 1.0 * size[0] / nt, rs = 1.0 * size[1] / ns;
+    const double ct = size[0] / 2, cs = size[1] / 2;
+    memset(disp, 0, sizeof(float) * (size_t)nt * ns);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16)
+    for (int si = 0; si < ns; ++si)
+    for (int ti = 0; ti < nt; ++ti) {
+        for (int b = 0; b < nth; ++b) {
+            const float th = theta[b];
+            double it = (ti + 0.5) * rt - ct, is = (si + 0.5) * rs - cs;
+            double t = it * (double)cosf(th) + is * (double)sinf(th);   /* float Theta */
+            double val = 0;
+            if ((t >= mint) && (t < maxt)) {
+                unsigned int t1 = (unsigned int)floor(fabs(t - T[0]) / tint), t2 = t1 + 1;
+                double d1 = fabs(t - T[t1]), d2 = fabs(T[t2] - t);
+                val = (d2 * rcov[(long)b * nt_det + t1] + d1 * rcov[(long)b * nt_det + t2]) / tint * thint;
+            }
+            long id = (long)si * nt + ti;
+            disp[id] = (float)((double)disp[id] + val);
+        }
+    }
+    free(rcov);
+    free(g);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Independent check: textbook alpha-Siddon line integral through a t,s,z   */
+/* grid (the merge-of-plane-crossings form of Siddon3D.m /                  */
+/* GenSysMatCircular3D.m), FP64.  Used by the tests as a second oracle that */
+/* shares no code with the reference walk above.                            */
+/* ------------------------------------------------------------------------ */
+OC_API double oc_siddon_line(const float *vol, int nt, int ns, int nz, const double res[3],
+                             const double src[3], const double dst[3])
+{
+    int n[3] = {nt, ns, nz};
+    double d[3] = {dst[0] - src[0], dst[1] - src[1], dst[2] - src[2]};
+    double a_in = 0.0, a_out = 1.0;
+    for (int k = 0; k < 3; ++k) {
+        double lo = 0.0, hi = n[k] * res[k];
+        if (d[k] == 0.0) {
+            if (src[k] <= lo || src[k] >= hi) return 0.0;
+            continue;
+        }
+        double a1 = (lo - src[k]) / d[k], a2 = (hi - src[k]) / d[k];
+        double amin = a1 < a2 ? a1 : a2, amax = a1 < a2 ? a2 : a1;
+        if (amin > a_in) a_in = amin;
+        if (amax < a_out) a_out = amax;
+    }
+    if (a_out <= a_in) return 0.0;
+    double len = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    /* next crossing alphas */
+    double anext[3], astep[3];
+    int idx[3], step[3];
+    double amid = a_in + 1e-9 * (a_out - a_in);
+    for (int k = 0; k < 3; ++k) {
+        double p = (src[k] + amid * d[k]) / res[k];
+        int i = (int)floor(p);
+        if (i < 0) i = 0;
+        if (i > n[k] - 1) i = n[k] - 1;
+        idx[k] = i;
+        if (d[k] > 0) { step[k] = 1; anext[k] = ((i + 1) * res[k] - src[k]) / d[k]; astep[k] = res[k] / d[k]; }
+        else if (d[k] < 0) { step[k] = -1; anext[k] = (i * res[k] - src[k]) / d[k]; astep[k] = -res[k] / d[k]; }
+        else { step[k] = 0; anext[k] = INFINITY; astep[k] = INFINITY; }
+    }
+    double acc = 0.0, a = a_in;
+    for (;;) {
+        int k = 0;
+        if (anext[1] < anext[k]) k = 1;
+        if (anext[2] < anext[k]) k = 2;
+        double an = anext[k] < a_out ? anext[k] : a_out;
+        if (an > a) acc += (an - a) * vol[(long)idx[2] * nt * ns + (long)idx[1] * nt + idx[0]];
+        a = an;
+        if (a >= a_out) break;
+        idx[k] += step[k];
+        anext[k] += astep[k];
+        if (idx[k] < 0 || idx[k] >= n[k]) break;
+    }
+    return acc * len;
+}
+
+/* Count of Siddon segments of each cone ray (the unit of the algorithmic
+   byte count of the forward projector).  Returns the total over all rays. */
+OC_API long long oc_cone_segments(int nt, int ns, int nz, const double *res, double ct, double cs,
+                                  double cz, const float *beta, const float *P, const float *xi,
+                                  int nb, int np, int nx, double D, int stride, int nthreads)
+{
+    set_threads(nthreads);
+    long long total = 0;
+    long nray = (long)nb * nx * np;
+    if (stride < 1) stride = 1;
+#pragma omp parallel for reduction(+:total) schedule(dynamic, 256)
+    for (long r = 0; r < nray; r += stride) {
+        int ip = (int)(r % np), ix = (int)((r / np) % nx), ib = (int)(r / ((long)np * nx));
+        double sb = sin((double)beta[ib]), cb = cos((double)beta[ib]);
+        double src[3] = {ct - D * sb, cs + D * cb, cz};
+        double d[3] = {P[ip] * cb + D * sb, P[ip] * sb - D * cb, (double)xi[ix]};
+        int n[3] = {nt, ns, nz};
+        double a_in = -1e300, a_out = 1e300;
+        int miss = 0;
+        for (int k = 0; k < 3; ++k) {
+            double lo = 0.0, hi = n[k] * res[k];
+            if (d[k] == 0.0) { if (src[k] <= lo || src[k] >= hi) miss = 1; continue; }
+            double a1 = (lo - src[k]) / d[k], a2 = (hi - src[k]) / d[k];
+            double amin = a1 < a2 ? a1 : a2, amax = a1 < a2 ? a2 : a1;
+            if (amin > a_in) a_in = amin;
+            if (amax < a_out) a_out = amax;
+        }
+        if (miss || a_out <= a_in) continue;
+        long long c = 1;
+        for (int k = 0; k < 3; ++k) {
+            double g0 = (src[k] + a_in * d[k]) / res[k], g1 = (src[k] + a_out * d[k]) / res[k];
+            double lo = g0 < g1 ? g0 : g1, hi = g0 < g1 ? g1 : g0;
+            long long cnt = (long long)ceil(hi) - (long long)floor(lo) - 1;
+            if (cnt > 0) c += cnt;
+        }
+        total += c;
+    }
+    return total * stride;
+}

@@ -1,0 +1,362 @@
+"""ctypes front end of the checker (TEST INFRASTRUCTURE ONLY).
+
+``Oracle`` wraps oracle/_build/libct_oracle.so, the FP64 CPU restatement of the
+reference operators (oracle/ct_oracle.c).  ``RefCPU`` wraps the reference's own
+kernels compiled as host code (oracle/_ref/, present only where the reference
+source tree was available at build time).  Only tests/, __graft_entry__.smoke()
+and bench.py's CPU arms may use this module; the product library never does.
+
+All array arguments are numpy arrays in the reference layouts:
+volume [z][s][t] (t fastest), cone sinogram [beta][xi][P] (P fastest),
+2D image [s][t], 2D sinogram [beta][P].
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i, _d = C.c_int, C.c_double
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Oracle:
+    """FP64 restatement of the reference operators (OpenMP over host cores)."""
+
+    def __init__(self, nthreads: int = 0):
+        lib = C.CDLL(str(_build.build_oracle()))
+        self.lib = lib
+        self.nthreads = nthreads or (os.cpu_count() or 1)
+        lib.oc_cone_fp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _i, _i, _i, _d, _d, _d,
+                                   _i, _i, _i, _d, _f64p, _i]
+        lib.oc_cone_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _d, _i, _i, _i, _f64p,
+                                   _i, _i, _i, _i]
+        lib.oc_sl_filter.argtypes = [_f32p, C.c_float, _i]
+        lib.oc_fdk_weight_apply.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _i, _d]
+        lib.oc_fbpfan_weight_apply.argtypes = [_f32p, _f32p, _f32p, _i, _i, _d]
+        lib.oc_fdk_filter.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _i, _d, _i, _i]
+        lib.oc_fdk_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _d, _i, _i, _i, _f64p,
+                                  _i, _i, _i, _i, _i]
+        lib.oc_fdk.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _d, _i, _i, _i, _f64p,
+                               _i, _i, _i, _i, _i, _i]
+        lib.oc_fan_fp.argtypes = [_f32p, _f64p, _f64p, _f64p, _i, _i, _d, _d, _i, _i, _d, _f64p, _i]
+        lib.oc_par_fp.argtypes = [_f32p, _f64p, _f64p, _f64p, _i, _i, _d, _d, _i, _i, _f64p, _i]
+        lib.oc_fan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i]
+        lib.oc_fbpfan_filter.argtypes = [_f32p, _f32p, _f32p, _i, _i, _d, _i, _i]
+        lib.oc_fbpfan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i]
+        lib.oc_fbpfan.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i, _i]
+        lib.oc_fbppar.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _i]
+        lib.oc_siddon_line.argtypes = [_f32p, _i, _i, _i, _f64p, _f64p, _f64p]
+        lib.oc_siddon_line.restype = C.c_double
+        lib.oc_cone_segments.argtypes = [_i, _i, _i, _f64p, _d, _d, _d, _f32p, _f32p, _f32p,
+                                         _i, _i, _i, _d, _i, _i]
+        lib.oc_cone_segments.restype = C.c_longlong
+
+    # -- 3D cone ------------------------------------------------------------
+    def cone_fp(self, vol, beta, P, xi, size, D):
+        """ProjectionCone_3D: vol [z][s][t] -> sinogram [beta][xi][P] (float32)."""
+        vol = _f32(vol)
+        nz, ns, nt = vol.shape
+        beta, P, xi = _f32(beta), _f32(P), _f32(xi)
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns, size[2] / nz])
+        out = np.zeros((len(beta), len(xi), len(P)), np.float32)
+        self.lib.oc_cone_fp(vol.ravel(), out.ravel(), beta, P, xi, nt, ns, nz, size[0] / 2, size[1] / 2,
+                            size[2] / 2, len(beta), len(P), len(xi), float(D), res, self.nthreads)
+        return out
+
+    def cone_bp(self, R, beta, P, xi, size, D, shape):
+        """Backprojection3D (BackPro): sinogram [beta][xi][P] -> vol [z][s][t]."""
+        nz, ns, nt = shape
+        R = _f32(R)
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_cone_bp(out.ravel(), R.ravel(), _f32(xi), _f32(P), _f32(beta), float(D), len(beta),
+                            len(P), len(xi), _f64(size), nt, ns, nz, self.nthreads)
+        return out
+
+    def sl_filter(self, pint, np_):
+        g = np.zeros(2 * np_ - 1, np.float32)
+        self.lib.oc_sl_filter(g, pint, np_)
+        return g
+
+    def fdk_weight_apply(self, R, P, xi, D):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fdk_weight_apply(out.ravel(), R.ravel(), _f32(P), _f32(xi), R.shape[0], len(P), len(xi),
+                                     float(D))
+        return out
+
+    def fbpfan_weight_apply(self, R, P, rscan):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fbpfan_weight_apply(out.ravel(), R.ravel(), _f32(P), R.shape[0], len(P), float(rscan))
+        return out
+
+    def fdk_filter(self, R, P, xi, D, mode=0):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        nb = R.shape[0]
+        self.lib.oc_fdk_filter(out.ravel(), R.ravel(), _f32(xi), _f32(P), nb, len(P), len(xi), float(D),
+                               int(mode), self.nthreads)
+        return out
+
+    def fdk_bp(self, rcov, beta, P, xi, size, D, shape, sticky=1):
+        nz, ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fdk_bp(out.ravel(), _f32(rcov).ravel(), _f32(xi), _f32(P), _f32(beta), float(D),
+                           len(beta), len(P), len(xi), _f64(size), nt, ns, nz, int(sticky), self.nthreads)
+        return out
+
+    def fdk(self, R, beta, P, xi, size, D, shape, filter_mode=1, sticky=1):
+        nz, ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fdk(out.ravel(), _f32(R).ravel(), _f32(xi), _f32(P), _f32(beta), float(D), len(beta),
+                        len(P), len(xi), _f64(size), nt, ns, nz, int(filter_mode), int(sticky),
+                        self.nthreads)
+        return out
+
+    # -- 2D -----------------------------------------------------------------
+    def fan_fp(self, img, beta, P, size, D):
+        """ProjectionFan_2D: img [s][t] -> sinogram [beta][P] (float64)."""
+        img = _f32(img)
+        ns, nt = img.shape
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns])
+        beta, P = _f64(beta), _f64(P)
+        out = np.zeros((len(beta), len(P)), np.float64)
+        self.lib.oc_fan_fp(img.ravel(), out.ravel(), beta, P, nt, ns, size[0] / 2, size[1] / 2,
+                           len(beta), len(P), float(D), res, self.nthreads)
+        return out
+
+    def par_fp(self, img, theta, trange, size):
+        """ProjectionParallel_2D: img [height][width] -> sinogram [theta][t] (float64)."""
+        img = _f32(img)
+        h, w = img.shape
+        size = _f64(size)
+        res = _f64([size[0] / h, size[1] / w])
+        theta, trange = _f64(theta), _f64(trange)
+        out = np.zeros((len(theta), len(trange)), np.float64)
+        self.lib.oc_par_fp(img.ravel(), out.ravel(), theta, trange, h, w, size[0] / 2, size[1] / 2,
+                           len(theta), len(trange), res, self.nthreads)
+        return out
+
+    def fan_bp(self, R, beta, P, size, shape, rscan):
+        """BackprojectionFan2D: sinogram [beta][P] -> img [s][t]."""
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fan_bp(out.ravel(), _f32(R).ravel(), _f32(P), _f32(beta), len(beta), len(P), _f64(size),
+                           nt, ns, float(rscan), self.nthreads)
+        return out
+
+    def fbpfan_filter(self, R, P, rscan, mode=0):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fbpfan_filter(out.ravel(), R.ravel(), _f32(P), R.shape[0], len(P), float(rscan),
+                                  int(mode), self.nthreads)
+        return out
+
+    def fbpfan_bp(self, rcov, beta, P, size, shape, rscan):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fbpfan_bp(out.ravel(), _f32(rcov).ravel(), _f32(P), _f32(beta), len(beta), len(P),
+                              _f64(size), nt, ns, float(rscan), self.nthreads)
+        return out
+
+    def fbpfan(self, R, beta, P, size, shape, rscan, filter_mode=1):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fbpfan(out.ravel(), _f32(R).ravel(), _f32(P), _f32(beta), len(beta), len(P), _f64(size),
+                           nt, ns, float(rscan), int(filter_mode), self.nthreads)
+        return out
+
+    def fbppar(self, R, theta, T, size, shape):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.lib.oc_fbppar(out.ravel(), _f32(R).ravel(), _f32(T), _f32(theta), len(theta), len(T),
+                           _f64(size), nt, ns, self.nthreads)
+        return out
+
+    # -- independent checks ---------------------------------------------------
+    def siddon_line(self, vol, size, src, dst):
+        vol = _f32(vol)
+        nz, ns, nt = vol.shape
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns, size[2] / nz])
+        return self.lib.oc_siddon_line(vol.ravel(), nt, ns, nz, res, _f64(src), _f64(dst))
+
+    def cone_segments(self, shape, size, beta, P, xi, D, stride=1):
+        nz, ns, nt = shape
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns, size[2] / nz])
+        return int(self.lib.oc_cone_segments(nt, ns, nz, res, size[0] / 2, size[1] / 2, size[2] / 2,
+                                             _f32(beta), _f32(P), _f32(xi), len(beta), len(P), len(xi),
+                                             float(D), int(stride), self.nthreads))
+
+
+class RefCPU:
+    """The reference's own kernel functions, compiled as host code (checker only)."""
+
+    def __init__(self):
+        libs = {}
+        for name, *_ in _build.REF_UNITS:
+            p = _build.REF_OUT / f"libref_{name}.so"
+            if not p.exists():
+                raise FileNotFoundError(f"{p} missing: run oracle/build.py where the reference tree exists")
+            libs[name] = C.CDLL(str(p))
+        self.libs = libs
+        L = libs
+        L["cone"].ref_cone_fp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _i, _i, _i, _d, _d, _d,
+                                          _i, _i, _i, _d, _f64p]
+        L["bp3d"].ref_cone_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _d, _i, _i, _i, _f64p,
+                                          _i, _i, _i]
+        L["fdk"].ref_fdk_G.argtypes = [_f32p, C.c_float, _i]
+        L["fdk"].ref_fdk_weight.argtypes = [_f32p, _f32p, _f32p, _i, _i, _i, _d]
+        L["fdk"].ref_fdk_conv.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _i]
+        L["fdk"].ref_fdk_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _d, _i, _i, _i, _f64p,
+                                        _i, _i, _i]
+        L["fan"].ref_fan_fp.argtypes = [_f32p, _f64p, _f64p, _f64p, _i, _i, _d, _d, _i, _i, _d, _f64p]
+        L["par"].ref_par_fp.argtypes = [_f32p, _f64p, _f64p, _f64p, _i, _i, _d, _d, _i, _i, _f64p]
+        L["fanbp"].ref_fan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d]
+        L["fbpfan"].ref_fbpfan_weight.argtypes = [_f32p, _f32p, _i, _i, _d]
+        L["fbpfan"].ref_fbpfan_conv.argtypes = [_f32p, _f32p, _f32p, _i, _i]
+        L["fbpfan"].ref_fbpfan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d]
+        L["fbppar"].ref_fbppar.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i]
+
+    def cone_fp(self, vol, beta, P, xi, size, D):
+        vol = _f32(vol)
+        nz, ns, nt = vol.shape
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns, size[2] / nz])
+        out = np.zeros((len(beta), len(xi), len(P)), np.float32)
+        self.libs["cone"].ref_cone_fp(vol.ravel(), out.ravel(), _f32(beta), _f32(P), _f32(xi), nt, ns, nz,
+                                      size[0] / 2, size[1] / 2, size[2] / 2, len(beta), len(P), len(xi),
+                                      float(D), res)
+        return out
+
+    def cone_bp(self, R, beta, P, xi, size, D, shape):
+        nz, ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.libs["bp3d"].ref_cone_bp(out.ravel(), _f32(R).ravel(), _f32(xi), _f32(P), _f32(beta), float(D),
+                                      len(beta), len(P), len(xi), _f64(size), nt, ns, nz)
+        return out
+
+    def sl_filter(self, pint, np_):
+        g = np.zeros(2 * np_ - 1, np.float32)
+        self.libs["fdk"].ref_fdk_G(g, pint, np_)
+        return g
+
+    def fdk_weight(self, R, P, xi, D):
+        R = _f32(R).copy()
+        self.libs["fdk"].ref_fdk_weight(R.ravel(), _f32(P), _f32(xi), R.shape[0], len(P), len(xi), float(D))
+        return R
+
+    def fdk_conv(self, Rw, P, xi):
+        Rw = _f32(Rw).copy()
+        out = np.zeros_like(Rw)
+        self.libs["fdk"].ref_fdk_conv(out.ravel(), Rw.ravel(), _f32(P), _f32(xi), Rw.shape[0], len(P), len(xi))
+        return out
+
+    def fdk_bp(self, rcov, beta, P, xi, size, D, shape):
+        nz, ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.libs["fdk"].ref_fdk_bp(out.ravel(), _f32(rcov).ravel(), _f32(xi), _f32(P), _f32(beta), float(D),
+                                    len(beta), len(P), len(xi), _f64(size), nt, ns, nz)
+        return out
+
+    def fan_fp(self, img, beta, P, size, D):
+        img = _f32(img)
+        ns, nt = img.shape
+        size = _f64(size)
+        res = _f64([size[0] / nt, size[1] / ns])
+        out = np.zeros((len(beta), len(P)), np.float64)
+        self.libs["fan"].ref_fan_fp(img.ravel(), out.ravel(), _f64(beta), _f64(P), nt, ns, size[0] / 2,
+                                    size[1] / 2, len(beta), len(P), float(D), res)
+        return out
+
+    def par_fp(self, img, theta, trange, size):
+        img = _f32(img)
+        h, w = img.shape
+        size = _f64(size)
+        res = _f64([size[0] / h, size[1] / w])
+        out = np.zeros((len(theta), len(trange)), np.float64)
+        self.libs["par"].ref_par_fp(img.ravel(), out.ravel(), _f64(theta), _f64(trange), h, w, size[0] / 2,
+                                    size[1] / 2, len(theta), len(trange), res)
+        return out
+
+    def fan_bp(self, R, beta, P, size, shape, rscan):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.libs["fanbp"].ref_fan_bp(out.ravel(), _f32(R).ravel(), _f32(P), _f32(beta), len(beta), len(P),
+                                      _f64(size), nt, ns, float(rscan))
+        return out
+
+    def fbpfan_weight(self, R, P, rscan):
+        R = _f32(R).copy()
+        self.libs["fbpfan"].ref_fbpfan_weight(R.ravel(), _f32(P), R.shape[0], len(P), float(rscan))
+        return R
+
+    def fbpfan_conv(self, Rw, P):
+        Rw = _f32(Rw).copy()
+        out = np.zeros_like(Rw)
+        self.libs["fbpfan"].ref_fbpfan_conv(out.ravel(), Rw.ravel(), _f32(P), Rw.shape[0], len(P))
+        return out
+
+    def fbpfan_bp(self, rcov, beta, P, size, shape, rscan):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.libs["fbpfan"].ref_fbpfan_bp(out.ravel(), _f32(rcov).ravel(), _f32(P), _f32(beta), len(beta),
+                                          len(P), _f64(size), nt, ns, float(rscan))
+        return out
+
+    def fbppar(self, R, theta, T, size, shape):
+        ns, nt = shape
+        out = np.zeros(shape, np.float32)
+        self.libs["fbppar"].ref_fbppar(out.ravel(), _f32(R).ravel(), _f32(T), _f32(theta), len(theta), len(T),
+                                       _f64(size), nt, ns)
+        return out
+
+
+def ref_available() -> bool:
+    return all((_build.REF_OUT / f"libref_{n}.so").exists() for n, *_ in _build.REF_UNITS)
+
+
+# -- analytic known-answer line integrals ------------------------------------
+def ellipsoid_line_integral(src, dst, ellipsoids):
+    """Exact line integral of a sum of constant-density ellipsoids along the
+    segment src->dst (extends the parallel-beam ellipse formula of
+    AnalyticProjectionParal.m:51-63 to 3D rays).  ellipsoids: rows of
+    (A, a, b, c, x0, y0, z0, phi) with phi the rotation about z (radians),
+    in the same world frame as src/dst."""
+    src = np.asarray(src, float)
+    d = np.asarray(dst, float) - src
+    total = 0.0
+    for A, a, b, c, x0, y0, z0, phi in ellipsoids:
+        cp, sp = np.cos(phi), np.sin(phi)
+        rot = np.array([[cp, sp, 0.0], [-sp, cp, 0.0], [0.0, 0.0, 1.0]])
+        o = rot @ (src - np.array([x0, y0, z0]))
+        v = rot @ d
+        s = np.array([1 / a, 1 / b, 1 / c])
+        o, v = o * s, v * s
+        qa, qb, qc = v @ v, 2 * o @ v, o @ o - 1
+        disc = qb * qb - 4 * qa * qc
+        if disc <= 0:
+            continue
+        r = np.sqrt(disc)
+        t0, t1 = (-qb - r) / (2 * qa), (-qb + r) / (2 * qa)
+        t0, t1 = max(t0, 0.0), min(t1, 1.0)
+        if t1 > t0:
+            total += A * (t1 - t0) * np.linalg.norm(d)
+    return total
