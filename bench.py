@@ -176,6 +176,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def small_geometry():
+    """Profiling case of the same kernels: 256^3, 90 views, 384x256 detector
+    (volume 64 MiB, sinogram 35 MB: inputs above L2 together, one launch ~ms)."""
+    from ctgb import geometry
+    g = geometry.config_cone_512()
+    return geometry.cone_from_physical((256, 256, 256), (200.0, 200.0, 150.0), 90, 384, 256, 1.6, 600.0, 1200.0,
+                                       name="cone_256_profile")
+
+
 def run_ours(args):
     import torch
     rank, world, local = _dist_env()
@@ -191,7 +200,7 @@ def run_ours(args):
     from ctgb import geometry, phantom, _lib
     from ctgb.device import ConePlan
     ctgb.load()
-    geom = geometry.config_cone_512()
+    geom = geometry.config_cone_512() if args.size == "full" else small_geometry()
     vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2), device=dev)
     plan = ConePlan(geom)
     proj = plan.new_sino(dev)
@@ -252,13 +261,16 @@ def run_ours(args):
                                   len(geom.beta), len(geom.P), len(geom.xi), vp(size), geom.nt, geom.ns, geom.nz),
                    "ct_BackPro")
 
-    e2e_step()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    if args.no_e2e:
+        t_e2e = float("nan")
+    else:
         e2e_step()
-    t_e2e = (time.perf_counter() - t0) / args.steps
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        t_e2e = (time.perf_counter() - t0) / args.steps
     if dist:
         t = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -293,11 +305,15 @@ def run_ours(args):
                 "traffic": tr, "kernel": dom, "peak_source": peak_kind,
                 "pair_frac": (fp_bytes + bp_bytes) / (t_fp + t_bp) / 1e9 / peak}
     cpu = cpu_sample(geom, vol.cpu().numpy()) if (world == 1 and not args.no_cpu) else None
+    if args.size != "full":
+        line_workload = f"{geom.name}: profiling case (not the benchmark workload)"
+    else:
+        line_workload = WORKLOAD
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+            "config": {"workload": line_workload, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (512 MiB volume, 566 MB sinogram, 2.3 GB packed quads)",
                        "phantom": "12 random ellipsoids, seed 2"},
             "roofline": roofline, "kernels": kern, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
@@ -315,6 +331,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
+    ap.add_argument("--size", choices=["full", "small"], default="full",
+                    help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

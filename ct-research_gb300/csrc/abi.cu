@@ -68,6 +68,17 @@ static int upload(DevBuf &b, const T *host, size_t n) {
     return CT_OK;
 }
 
+// List of grazing rays for the FP64 re-walk (ref_walk.cu); allocated on first use.
+constexpr int kGrazeCap = 1 << 16;
+static int graze_list(DevBuf &b, GrazeList &gl) {
+    int s = b.ensure(sizeof(unsigned long long) * kGrazeCap + sizeof(int) * 4);
+    if (s) return s;
+    gl.rays = b.as<unsigned long long>();
+    gl.count = reinterpret_cast<int *>(b.as<unsigned long long>() + kGrazeCap);
+    gl.cap = kGrazeCap;
+    return CT_OK;
+}
+
 // Shepp-Logan-form taps exactly as GFunction computes them (FDK.cu:6-19):
 // double arithmetic, stored as float.
 static std::vector<float> sl_taps(float pint, int np) {
@@ -95,7 +106,7 @@ using namespace ct;
 struct ct_cone_plan {
     ConeGeom g{};
     DevBuf trig, P, xi;
-    DevBuf quads, rcov, G, wtab, norms;
+    DevBuf quads, rcov, G, wtab, norms, graze;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     // host copies of the geometry (drop-in cache key)
@@ -103,7 +114,7 @@ struct ct_cone_plan {
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
         trig.release(); P.release(); xi.release();
-        quads.release(); rcov.release(); G.release(); wtab.release(); norms.release();
+        quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
     }
 };
 
@@ -191,18 +202,25 @@ int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode) 
 
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
-    return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes;
+    return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
+           plan->graze.bytes;
 }
 
 int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stream) {
     CT_REQUIRE(plan && d_vol && d_proj, "ct_cone_fp: null argument");
-    return cone_fp_launch(plan->g, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, as_stream(stream));
+    GrazeList gl;
+    int s = graze_list(plan->graze, gl);
+    if (s) return s;
+    return cone_fp_launch(plan->g, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl, as_stream(stream));
 }
 
 int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b, const float *d_rowsum,
                         float eps, float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(plan && d_vol && d_b && d_out && d_norms, "ct_cone_fp_residual: null argument");
-    return cone_fp_launch(plan->g, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, as_stream(stream));
+    GrazeList gl;
+    int s = graze_list(plan->graze, gl);
+    if (s) return s;
+    return cone_fp_launch(plan->g, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
 static int cone_bp_common(ct_cone_plan *plan, const float *d_proj, float *d_vol, int weighting,
@@ -228,11 +246,9 @@ int ct_cone_bp_update(ct_cone_plan *plan, const float *d_proj, const float *d_co
     return cone_bp_common(plan, d_proj, d_vol, 0, d_colsum, eps, lambda, lo, hi, true, as_stream(stream));
 }
 
-int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream) {
-    CT_REQUIRE(plan && d_proj && d_vol, "ct_cone_fdk: null argument");
+static int cone_fdk_filter_into(ct_cone_plan *plan, const float *d_proj, float *d_out, cudaStream_t st) {
     ConeGeom &g = plan->g;
-    CT_REQUIRE(g.np >= 2 && g.nx >= 2, "ct_cone_fdk: detector needs at least 2x2 samples");
-    cudaStream_t st = as_stream(stream);
+    CT_REQUIRE(g.np >= 2 && g.nx >= 2, "FDK: detector needs at least 2x2 samples");
     int s;
     if (!plan->G.ptr) {
         std::vector<float> taps = sl_taps(g.pint, g.np);
@@ -246,7 +262,6 @@ int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *str
             }
         if ((s = upload(plan->wtab, w.data(), w.size()))) return s;
     }
-    if ((s = plan->rcov.ensure(sizeof(float) * (size_t)g.nb * g.nx * g.np))) return s;
     RowFilter f{};
     f.nrow = g.nb * g.nx;
     f.np = g.np;
@@ -259,9 +274,29 @@ int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *str
     f.limit = 2048;      // FDK.h:24 Filterlengthlimit
     f.row_block = 256;   // FDK.h:23 blockX
     f.rowmod = g.nx;
-    if ((s = row_filter_launch(f, d_proj, plan->rcov.as<float>(), st))) return s;
-    return cone_bp_common(plan, plan->rcov.as<float>(), d_vol, plan->fdk_bp == CT_FDK_BP_STICKY ? 2 : 1,
-                          nullptr, 0.f, 0.f, 0.f, 0.f, false, st);
+    return row_filter_launch(f, d_proj, d_out, st);
+}
+
+int ct_cone_fdk_filter(ct_cone_plan *plan, const float *d_proj, float *d_filtered, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_filtered, "ct_cone_fdk_filter: null argument");
+    return cone_fdk_filter_into(plan, d_proj, d_filtered, as_stream(stream));
+}
+
+int ct_cone_fdk_bp(ct_cone_plan *plan, const float *d_filtered, float *d_vol, void *stream) {
+    CT_REQUIRE(plan && d_filtered && d_vol, "ct_cone_fdk_bp: null argument");
+    CT_REQUIRE(plan->g.np >= 2 && plan->g.nx >= 2, "ct_cone_fdk_bp: detector needs at least 2x2 samples");
+    return cone_bp_common(plan, d_filtered, d_vol, plan->fdk_bp == CT_FDK_BP_STICKY ? 2 : 1, nullptr, 0.f, 0.f,
+                          0.f, 0.f, false, as_stream(stream));
+}
+
+int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream) {
+    CT_REQUIRE(plan && d_proj && d_vol, "ct_cone_fdk: null argument");
+    ConeGeom &g = plan->g;
+    cudaStream_t st = as_stream(stream);
+    int s;
+    if ((s = plan->rcov.ensure(sizeof(float) * (size_t)g.nb * g.nx * g.np))) return s;
+    if ((s = cone_fdk_filter_into(plan, d_proj, plan->rcov.as<float>(), st))) return s;
+    return ct_cone_fdk_bp(plan, plan->rcov.as<float>(), d_vol, stream);
 }
 
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream) {
@@ -270,7 +305,8 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
     int s = plan->norms.ensure(2 * sizeof(double));
     if (s) return s;
     CT_CUDA(cudaMemsetAsync(plan->norms.ptr, 0, 2 * sizeof(double), st), "memset");
-    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, st)))
+    GrazeList gl{};
+    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, gl, st)))
         return s;
     double h = 0;
     CT_CUDA(cudaMemcpyAsync(&h, plan->norms.ptr, sizeof(double), cudaMemcpyDeviceToHost, st), "copy");
@@ -286,11 +322,11 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
 // ---------------------------------------------------------------------------
 struct ct_fan_plan {
     FanGeom g{};
-    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov;
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze;
     std::vector<float> hPf;
     ~ct_fan_plan() {
         trig_d.release(); Pd.release(); trig_f.release(); Pf.release();
-        G.release(); wtab.release(); rcov.release();
+        G.release(); wtab.release(); rcov.release(); graze.release();
     }
 };
 
@@ -364,13 +400,19 @@ int ct_fan_plan_destroy(ct_fan_plan *plan) {
 
 int ct_fan_fp(ct_fan_plan *plan, const float *d_img, float *d_proj, void *stream) {
     CT_REQUIRE(plan && d_img && d_proj, "ct_fan_fp: null argument");
-    return fan_fp_launch(plan->g, d_img, d_proj, nullptr, nullptr, 0.f, nullptr, 0, as_stream(stream));
+    GrazeList gl;
+    int s = graze_list(plan->graze, gl);
+    if (s) return s;
+    return fan_fp_launch(plan->g, d_img, d_proj, nullptr, nullptr, 0.f, nullptr, 0, gl, as_stream(stream));
 }
 
 int ct_fan_fp_residual(ct_fan_plan *plan, const float *d_img, const float *d_b, const float *d_rowsum, float eps,
                        float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(plan && d_img && d_b && d_out && d_norms, "ct_fan_fp_residual: null argument");
-    return fan_fp_launch(plan->g, d_img, d_out, d_b, d_rowsum, eps, d_norms, 1, as_stream(stream));
+    GrazeList gl;
+    int s = graze_list(plan->graze, gl);
+    if (s) return s;
+    return fan_fp_launch(plan->g, d_img, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
 int ct_fan_bp(ct_fan_plan *plan, const float *d_proj, float *d_img, void *stream) {
@@ -540,7 +582,9 @@ static int fan2d_run(ct_fan_plan *pl, int which, const void *in, void *out, int 
     cudaError_t e = cudaMemcpy(a.ptr, in, (fp ? nimg : nsino) * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) s = cuda_status(e, "H2D");
     if (!s) {
-        if (fp) s = fan_fp_launch(g, a.as<float>(), b.ptr, nullptr, nullptr, 0.f, nullptr, 3, 0);
+        GrazeList gl;
+        if (fp && !(s = graze_list(pl->graze, gl)))
+            s = fan_fp_launch(g, a.as<float>(), b.ptr, nullptr, nullptr, 0.f, nullptr, 3, gl, 0);
         else if (which == 1) s = fan_bp_launch(g, a.as<float>(), b.as<float>(), 0, nullptr, 0, 0, 0, 0, false, 0);
         else s = ct_fan_fbp(pl, a.as<float>(), b.as<float>(), filter_mode, nullptr);
     }

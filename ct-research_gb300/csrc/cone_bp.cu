@@ -51,22 +51,82 @@ pack_quads_kernel(const float *__restrict__ R, float4 *__restrict__ Q, int nb, i
 
 enum { W_CHORD = 0, W_FDK_ZERO = 1, W_FDK_STICKY = 2 };
 
+// FP64 re-evaluation of the reference's detector-range tests for one column
+// and view (Backprojection3D.cu:31-43 and :66-71, FDK.cu:80-100):
+// P in [minP, maxP) and xi(z) in [minXigama, maxXigama).  Used only when the
+// FP32 decision lies within rounding distance of a detector edge; it matters
+// most for the sticky FDK value, which is taken at the last in-range z.
+__device__ __noinline__ void range_fp64(const ConeGeom &g, int ti, int si, double sb, double cb, bool &pin,
+                                        int &zlo, int &zhi) {
+    const double it = (ti + 0.5) * g.res[0] - 0.5 * g.size[0];
+    const double is = (si + 0.5) * g.res[1] - 0.5 * g.size[1];
+    const double dect_t = it * cb + is * sb;
+    const double dect_s = -it * sb + is * cb;
+    const double lr = g.D / (g.D - dect_s);
+    const double P = dect_t * lr;
+    pin = (P >= (double)g.minp) && (P < (double)g.maxp);
+    const double rz = g.res[2], cz = 0.5 * g.size[2];
+    const double mnx = g.minx, mxx = g.maxx;
+    int lo = min(max(zlo, 0), g.nz);
+    while (lo > 0 && ((lo - 1 + 0.5) * rz - cz) * lr >= mnx) --lo;
+    while (lo < g.nz && !(((lo + 0.5) * rz - cz) * lr >= mnx)) ++lo;
+    int hi = min(max(zhi, -1), g.nz - 1);
+    while (hi + 1 < g.nz && ((hi + 1 + 0.5) * rz - cz) * lr < mxx) ++hi;
+    while (hi >= 0 && !(((hi + 0.5) * rz - cz) * lr < mxx)) --hi;
+    zlo = lo;
+    zhi = hi;
+}
+
+// The reference's chord construction for one voxel-view in FP64
+// (Backprojection3D.cu:243-281): false when no low face of the voxel holds the
+// entry point of the source->centre line, in which case the reference returns
+// and the rest of the column gets nothing from this view.  Each operation is
+// rounded separately (no FMA contraction), as the host build of that code is.
+__device__ __noinline__ bool chord_entry_found(const ConeGeom &g, int ti, int si, int zi, double sb, double cb) {
+    const double EPS = 1e-15;
+    const double ct = g.size[0] / 2, cs = g.size[1] / 2, cz = g.size[2] / 2;
+    const double rt = g.res[0], rs = g.res[1], rz = g.res[2];
+    const double it = __dsub_rn(__dmul_rn(ti + 0.5, rt), ct);
+    const double is = __dsub_rn(__dmul_rn(si + 0.5, rs), cs);
+    const double iz = __dsub_rn(__dmul_rn(zi + 0.5, rz), cz);
+    const double st = __dsub_rn(ct, __dmul_rn(g.D, sb)), ss = __dadd_rn(cs, __dmul_rn(g.D, cb)), sz = cz;
+    const double et = __dadd_rn(it, ct), es = __dadd_rn(is, cs), ez = __dadd_rn(iz, cz);
+    const double tlo = __dmul_rn((double)ti, rt), thi = __dmul_rn((double)(ti + 1), rt);
+    const double slo = __dmul_rn((double)si, rs), shi = __dmul_rn((double)(si + 1), rs);
+    const double zlo = __dmul_rn((double)zi, rz), zhi = __dmul_rn((double)(zi + 1), rz);
+    const double dt = __dsub_rn(et, st), ds = __dsub_rn(es, ss), dz = __dsub_rn(ez, sz);
+    const double dte = __dadd_rn(dt, EPS), dse = __dadd_rn(ds, EPS), dze = __dadd_rn(dz, EPS);
+    auto hit = [](double a0, double off, double d1, double de) {   // a0 + off * d1 / de
+        return __dadd_rn(a0, __ddiv_rn(__dmul_rn(off, d1), de));
+    };
+    const double tlo_s = hit(ss, __dsub_rn(tlo, st), ds, dte), tlo_z = hit(sz, __dsub_rn(tlo, st), dz, dte);
+    if (tlo_s >= slo && tlo_s <= shi && tlo_z >= zlo && tlo_z <= zhi) return true;
+    const double slo_t = hit(st, __dsub_rn(slo, ss), dt, dse), slo_z = hit(sz, __dsub_rn(slo, ss), dz, dse);
+    if (slo_t >= tlo && slo_t <= thi && slo_z >= zlo && slo_z <= zhi) return true;
+    const double zlo_t = hit(st, __dsub_rn(zlo, sz), dt, dze), zlo_s = hit(ss, __dsub_rn(zlo, sz), ds, dze);
+    return zlo_t >= tlo && zlo_t <= thi && zlo_s >= slo && zlo_s <= shi;
+}
+
 template <int WMODE, bool UPDATE>
 __global__ void __launch_bounds__(BP_BX * BP_BY)
 cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict__ vol,
                const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
+    // detector-row coordinate pairs (xi[x], xi[x+1]) for the interpolation weights
+    extern __shared__ float2 xpair[];
+    const int tid = threadIdx.x + BP_BX * threadIdx.y;
+    for (int x = tid; x < g.nx - 1; x += BP_BX * BP_BY) xpair[x] = make_float2(g.xi[x], g.xi[x + 1]);
+    __syncthreads();
+
     const int ti = blockIdx.x * BP_BX + threadIdx.x;
     const int si = blockIdx.y * BP_BY + threadIdx.y;
     const int z0 = blockIdx.z * BP_ZC;
     if (ti >= g.nt || si >= g.ns) return;
 
-    const float rt = (float)g.res[0], rs = (float)g.res[1], rz = (float)g.res[2];
-    const float ct_ = (float)(0.5 * g.size[0]), cs_ = (float)(0.5 * g.size[1]), cz_ = (float)(0.5 * g.size[2]);
+    const float rz = (float)g.res[2];
     const float it = (float)((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
     const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
     const float D = (float)g.D;
     const float ipint = 1.0f / g.pint, ixint = 1.0f / g.xint;
-    (void)ct_; (void)cs_; (void)rt; (void)rs;
 
     float acc[BP_ZC];
     float zg[BP_ZC], zq[BP_ZC];   // per z: h_z / |iz| and iz^2 (chord weight)
@@ -77,7 +137,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         zg[k] = 0.5f * rz / fabsf(iz);
         zq[k] = iz * iz;
     }
-    const float ht = 0.5f * (float)g.res[0], hs = 0.5f * (float)g.res[1];
+    const float ht = 0.5f * (float)g.res[0], hs = 0.5f * (float)g.res[1], hz = 0.5f * rz;
+    const float czf = (float)(0.5 * g.size[2]);
     const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);   // iz at z = 0
     const long long vstride = (long long)g.nx * g.np;
 
@@ -88,32 +149,54 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         const float dect_s = fmaf(is, cb, -it * sb);
         const float lr = D / (D - dect_s);
         const float P = dect_t * lr;
-        if (!(P >= g.minp && P < g.maxp)) continue;   // whole column off the detector
-        // detector column and its interpolation weight
-        const float pf = (P - g.p0) * g.psgn * ipint;
-        int p1 = __float2int_rd(pf);
-        p1 = min(max(p1, 0), g.np - 2);
-        const float fp = pf - (float)p1;
+        bool pin = P >= g.minp && P < g.maxp;
         // xi(z) = (x_base + z rz) * lr; detector rows in range for z in [zlo, zhi]
         const float xslope = rz * lr, xoff = x_base * lr;
         const float zlo_f = (g.minx - xoff) / xslope, zhi_f = (g.maxx - xoff) / xslope;
         int zlo = (int)ceilf(zlo_f);             // first z with xi >= minx
         int zhi = (int)ceilf(zhi_f) - 1;         // last z with xi < maxx
-        // fractional row index as a linear function of z
-        const float B = xslope * g.xsgn * ixint;
-        const float A = (xoff - g.x0) * g.xsgn * ixint;
+        // FP32 rounding is ~1e-4 in z units and ~3e-5 mm in P: re-decide in FP64 near an edge
+        const bool near_edge = fabsf(zlo_f - rintf(zlo_f)) < 1e-3f || fabsf(zhi_f - rintf(zhi_f)) < 1e-3f ||
+                               fabsf(P - g.minp) < 1e-3f || fabsf(P - g.maxp) < 1e-3f;
+        if (near_edge) range_fp64(g, ti, si, tr.x, tr.y, pin, zlo, zhi);
+        if (!pin) continue;   // whole column off the detector for this view
+        if (WMODE == W_FDK_STICKY && zhi < zlo) continue;
+        // detector column: index as floor(|P - P0| / PInt), weights from the
+        // domain values (Backprojection3D.cu:73-83)
+        int p1 = (int)(fabsf(P - g.p0) * ipint);
+        p1 = min(max(p1, 0), g.np - 2);
+        const float wq1 = fabsf(P - __ldg(g.P + p1)) * ipint;        // weight of column p1+1
+        const float wq0 = fabsf(__ldg(g.P + p1 + 1) - P) * ipint;    // weight of column p1
         const float4 *Qv = Q + (long long)v * vstride + p1;
 
         float wv = 1.0f, mts = 0.0f, qq = 0.0f;
+        int zab = 0x7fffffff;   // first z dropped by the reference's early return
         if (WMODE == W_CHORD) {
             const float dt = it + D * sb, ds = is - D * cb;
-            mts = fminf(ht / fabsf(dt), hs / fabsf(ds));
+            const float mt = ht / fabsf(dt), ms = hs / fabsf(ds);
+            mts = fminf(mt, ms);
             qq = fmaf(dt, dt, ds * ds);
+            // The source->centre line passes near a voxel edge when two faces'
+            // parameters tie; only then can the reference's FP64 face tests all
+            // fail.  Detect ties in FP32 with a wide margin, decide in FP64.
+            const bool tie_ts = fabsf(mt - ms) <= 1e-5f * mts;
+            const float ztie = hz / mts;   // |iz| where the z faces tie with mts
+            const float zc1 = (czf + ztie) / rz - 0.5f, zc2 = (czf - ztie) / rz - 0.5f;
+            const float r1 = rintf(zc1), r2 = rintf(zc2);
+            const bool tz1 = fabsf(zc1 - r1) < 1e-3f && r1 >= (float)zlo && r1 <= (float)zhi;
+            const bool tz2 = fabsf(zc2 - r2) < 1e-3f && r2 >= (float)zlo && r2 <= (float)zhi;
+            if (tie_ts) {
+                // t/s faces limit the chord where |iz| <= ztie: check those z in order
+                for (int z = max(zlo, 0); z <= min(zhi, g.nz - 1); ++z) {
+                    const float iz = fmaf((float)z, rz, x_base);
+                    if (fabsf(iz) > ztie * (1.0f + 1e-5f)) continue;
+                    if (!chord_entry_found(g, ti, si, z, tr.x, tr.y)) { zab = z; break; }
+                }
+            }
+            if (tz1 && (int)r1 < zab && !chord_entry_found(g, ti, si, (int)r1, tr.x, tr.y)) zab = (int)r1;
+            if (tz2 && (int)r2 < zab && !chord_entry_found(g, ti, si, (int)r2, tr.x, tr.y)) zab = (int)r2;
         } else {
             wv = lr * lr * g.bint;
-        }
-        if (WMODE == W_FDK_STICKY) {
-            if (zhi < zlo) continue;
         }
 #pragma unroll
         for (int k = 0; k < BP_ZC; ++k) {
@@ -123,14 +206,17 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
                 in = z >= zlo;
                 z = min(z, zhi);
             }
-            const float xf = fmaf((float)z, B, A);
-            int x1 = __float2int_rd(xf);
+            if (WMODE == W_CHORD) in = in && (z < zab);
+            const float xi = fmaf((float)z, xslope, xoff);
+            int x1 = (int)(fabsf(xi - g.x0) * ixint);
             x1 = min(max(x1, 0), g.nx - 2);
-            const float fr = xf - (float)x1;
+            const float2 xd = xpair[x1];
+            const float wx1 = fabsf(xi - xd.x) * ixint;     // weight of row x1+1
+            const float wx0 = fabsf(xd.y - xi) * ixint;     // weight of row x1
             const float4 q = __ldg(Qv + (long long)x1 * g.np);
-            const float top = fmaf(fp, q.y - q.x, q.x);
-            const float bot = fmaf(fp, q.w - q.z, q.z);
-            const float val = fmaf(fr, bot - top, top);
+            const float top = fmaf(wq0, q.x, wq1 * q.y);
+            const float bot = fmaf(wq0, q.z, wq1 * q.w);
+            const float val = fmaf(wx0, top, wx1 * bot);
             float w;
             if (WMODE == W_CHORD) {
                 w = 2.0f * fminf(mts, zg[k]) * sqrtf(qq + zq[k]);
@@ -173,8 +259,10 @@ int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting
     CT_REQUIRE(g.np >= 2 && g.nx >= 2, "cone_bp: detector needs at least 2x2 samples");
     dim3 block(BP_BX, BP_BY);
     dim3 grid((g.nt + BP_BX - 1) / BP_BX, (g.ns + BP_BY - 1) / BP_BY, (g.nz + BP_ZC - 1) / BP_ZC);
+    const size_t smem = sizeof(float2) * (size_t)g.nx;
+    CT_REQUIRE(smem <= 48 * 1024, "cone_bp: at most 6144 detector rows");
 #define CT_BP_CASE(W, U)                                                                     \
-    cone_bp_kernel<W, U><<<grid, block, 0, st>>>(g, Q, vol, colsum, eps, lambda, lo, hi)
+    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, vol, colsum, eps, lambda, lo, hi)
     if (update) {
         if (weighting == W_CHORD) CT_BP_CASE(W_CHORD, true);
         else if (weighting == W_FDK_ZERO) CT_BP_CASE(W_FDK_ZERO, true);

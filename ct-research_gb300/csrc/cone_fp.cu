@@ -14,7 +14,7 @@
 // assignment at the box boundary needs it), then the walk runs in FP32
 // registers (siddon.cuh).  The walk is unrolled by four so four gathers are
 // in flight per thread.
-#include "cone_geom.cuh"
+#include "kernels.cuh"
 #include "siddon.cuh"
 
 namespace ct {
@@ -42,7 +42,7 @@ template <int MODE>
 __global__ void __launch_bounds__(FP_BX * FP_BY)
 cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, float *__restrict__ out,
                const float *__restrict__ b, const float *__restrict__ rowsum, float eps,
-               double *__restrict__ norms) {
+               double *__restrict__ norms, const GrazeList gl) {
     const int p = blockIdx.x * FP_BX + threadIdx.x;
     const int x = blockIdx.y * FP_BY + threadIdx.y;
     const int v = blockIdx.z;
@@ -56,6 +56,10 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, float *__restric
         if (MODE == 2) {
             r2 = hit ? (double)w.nseg : 0.0;
         } else {
+            if (hit && w.grazing) {
+                const int slot = atomicAdd(gl.count, 1);
+                if (slot < gl.cap) gl.rays[slot] = (unsigned long long)o;
+            }
             const float val = hit ? ray_integral(w, vol, nmax) : 0.0f;
             if (MODE == 0) {
                 out[o] = val;
@@ -80,17 +84,19 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, float *__restric
 }  // namespace
 
 int cone_fp_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
-                   float eps, double *norms, int mode, cudaStream_t st) {
+                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
     dim3 block(FP_BX, FP_BY);
     dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, g.nb);
     CT_REQUIRE(g.nb <= 65535, "cone_fp: at most 65535 views per launch");
+    if (mode != 2) CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
     if (mode == 0)
-        cone_fp_kernel<0><<<grid, block, 0, st>>>(g, vol, out, nullptr, nullptr, 0.0f, nullptr);
+        cone_fp_kernel<0><<<grid, block, 0, st>>>(g, vol, out, nullptr, nullptr, 0.0f, nullptr, gl);
     else if (mode == 1)
-        cone_fp_kernel<1><<<grid, block, 0, st>>>(g, vol, out, b, rowsum, eps, norms);
+        cone_fp_kernel<1><<<grid, block, 0, st>>>(g, vol, out, b, rowsum, eps, norms, gl);
     else
-        cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, 0.0f, norms);
+        cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, 0.0f, norms, gl);
     CT_LAUNCH_CHECK("cone_fp_kernel");
+    if (mode != 2) return cone_fixup_launch(g, vol, out, b, rowsum, eps, norms, mode, gl.rays, gl.count, gl.cap, st);
     return CT_OK;
 }
 

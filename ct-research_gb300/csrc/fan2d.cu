@@ -32,7 +32,7 @@ template <typename OutT, int MODE>
 __global__ void __launch_bounds__(F2_BLOCK)
 fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__ out,
               const float *__restrict__ b, const float *__restrict__ rowsum, float eps,
-              double *__restrict__ norms) {
+              double *__restrict__ norms, const GrazeList gl) {
     const long long r = (long long)blockIdx.x * F2_BLOCK + threadIdx.x;
     const bool active = r < (long long)g.nb * g.np;
     double r2 = 0.0, b2 = 0.0;
@@ -60,7 +60,13 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
         d[2] = 0.0;
         RayWalk w;
         float val = 0.0f;
-        if (siddon_setup(src, d, n, res, w)) val = ray_integral(w, img, g.nt * g.ns - 1);
+        if (siddon_setup(src, d, n, res, w)) {
+            val = ray_integral(w, img, g.nt * g.ns - 1);
+            if (w.grazing) {
+                const int slot = atomicAdd(gl.count, 1);
+                if (slot < gl.cap) gl.rays[slot] = (unsigned long long)r;
+            }
+        }
         if (MODE == 0) {
             out[r] = (OutT)val;
         } else {
@@ -108,12 +114,14 @@ fan_bp_kernel(const FanGeom g, const float *__restrict__ R, float *__restrict__ 
         }
         float val = 0.0f;
         if (Pd >= g.minp && Pd < g.maxp) {
-            const float pf = (Pd - g.p0) * g.psgn * ipint;
-            int p1 = __float2int_rd(pf);
+            // index floor(|P - P0| / PInt), weights from the domain values
+            // (BackprojectionFan2D.cu:44-53)
+            int p1 = (int)(fabsf(Pd - g.p0) * ipint);
             p1 = min(max(p1, 0), g.np - 2);
-            const float fp = pf - (float)p1;
+            const float w1 = fabsf(Pd - __ldg(g.Pf + p1)) * ipint;
+            const float w0 = fabsf(__ldg(g.Pf + p1 + 1) - Pd) * ipint;
             const float *Rv = R + (long long)v * g.np + p1;
-            val = fmaf(fp, __ldg(Rv + 1) - __ldg(Rv), __ldg(Rv));
+            val = fmaf(w0, __ldg(Rv), w1 * __ldg(Rv + 1));
         }
         if (WMODE == BP2_BACKPROJ) {
             // unit direction of the source->detector-point line and its far end
@@ -152,17 +160,19 @@ fan_bp_kernel(const FanGeom g, const float *__restrict__ R, float *__restrict__ 
 
 // mode 0: forward projection (float); 1: residual (float); 3: forward projection into double
 int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
-                  float eps, double *norms, int mode, cudaStream_t st) {
+                  float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
     const long long nray = (long long)g.nb * g.np;
     const unsigned blocks = (unsigned)((nray + F2_BLOCK - 1) / F2_BLOCK);
+    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
     if (mode == 0)
-        fan_fp_kernel<float, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (float *)out, nullptr, nullptr, 0.f, nullptr);
+        fan_fp_kernel<float, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (float *)out, nullptr, nullptr, 0.f, nullptr, gl);
     else if (mode == 1)
-        fan_fp_kernel<float, 1><<<blocks, F2_BLOCK, 0, st>>>(g, img, (float *)out, b, rowsum, eps, norms);
+        fan_fp_kernel<float, 1><<<blocks, F2_BLOCK, 0, st>>>(g, img, (float *)out, b, rowsum, eps, norms, gl);
     else
-        fan_fp_kernel<double, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (double *)out, nullptr, nullptr, 0.f, nullptr);
+        fan_fp_kernel<double, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (double *)out, nullptr, nullptr, 0.f, nullptr, gl);
     CT_LAUNCH_CHECK("fan_fp_kernel");
-    return CT_OK;
+    return fan_fixup_launch(g, img, out, mode == 3, b, rowsum, eps, norms, mode == 1 ? 1 : 0, gl.rays, gl.count,
+                            gl.cap, st);
 }
 
 // wmode: 0 BackprojectionFan2D weight, 1 FBPfan, 2 FBPpara

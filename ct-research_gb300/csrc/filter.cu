@@ -80,15 +80,24 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
             }
             __syncthreads();
             for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+                // The reference rounds each float*float product to float and sums
+                // in double (FDK.cu:41-45).  Here: the same rounded products,
+                // summed as an unevaluated pair (s + c) with the TwoSum error-free
+                // transformation (Knuth), flushed into a double every 256 taps.
                 double dacc = 0.0;
-                float acc = 0.0f;
+                float sh = 0.0f, sl = 0.0f;
                 const float *gp = G + (np - 1) + p;
                 int n = 0;
                 for (int q = g0; q < g1; ++q) {
-                    acc = fmaf(mix[q], gp[-q], acc);
-                    if (++n == 128) { dacc += acc; acc = 0.0f; n = 0; }
+                    const float prod = __fmul_rn(mix[q], gp[-q]);
+                    const float t = __fadd_rn(sh, prod);
+                    const float bp = __fsub_rn(t, sh);
+                    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(prod, bp));
+                    sh = t;
+                    sl = __fadd_rn(sl, err);
+                    if (++n == 256) { dacc += (double)sh + (double)sl; sh = sl = 0.0f; n = 0; }
                 }
-                dacc += acc;
+                dacc += (double)sh + (double)sl;
                 o[p] = (float)((double)o[p] + (double)f.pint * dacc);
             }
             __syncthreads();

@@ -32,15 +32,29 @@ struct RowFilter {
     int tile, limit, row_block, rowmod;   // reference tiling
 };
 
+// Rays that graze a grid plane, listed by the fast projectors for the FP64
+// re-walk of ref_walk.cu.  count is reset by the launcher.
+struct GrazeList {
+    unsigned long long *rays;
+    int *count;
+    int cap;
+};
+
 int cone_fp_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
-                   float eps, double *norms, int mode, cudaStream_t st);
+                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
+int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
+                      float eps, double *norms, int mode, const unsigned long long *list, const int *count, int cap,
+                      cudaStream_t st);
+int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_double, const float *b,
+                     const float *rowsum, float eps, double *norms, int mode, const unsigned long long *list,
+                     const int *count, int cap, cudaStream_t st);
 size_t cone_quads_bytes(const ConeGeom &g);
 int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, cudaStream_t st);
 int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting, const float *colsum,
                    float eps, float lambda, float lo, float hi, bool update, cudaStream_t st);
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st);
 int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
-                  float eps, double *norms, int mode, cudaStream_t st);
+                  float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_bp_launch(const FanGeom &g, const float *R, float *img, int wmode, const float *colsum, float eps,
                   float lambda, float lo, float hi, bool update, cudaStream_t st);
 int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int nz, int iters, float step,

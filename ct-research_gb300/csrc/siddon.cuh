@@ -23,6 +23,7 @@ struct RayWalk {
     int nseg;              // segments along the ray
     float L;               // exit parameter
     float scale;           // |d| in mm per parameter unit
+    bool grazing;          // runs along a grid plane to FP64 precision (see ref_walk.cu)
 };
 
 // FP64 slab test against the box [0, n*res] and walk set-up for the line
@@ -31,6 +32,7 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
                                              const double res[3], RayWalk &w) {
     double inv[3];
     double a_in = -1.0e300, a_out = 1.0e300;
+    int ax_in = -1, ax_out = -1;   // axes whose faces the line enters and leaves through
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const double hi = n[a] * res[a];
@@ -38,8 +40,9 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
             inv[a] = drcp(d[a]);
             const double t0 = (0.0 - src[a]) * inv[a];
             const double t1 = (hi - src[a]) * inv[a];
-            a_in = fmax(a_in, fmin(t0, t1));
-            a_out = fmin(a_out, fmax(t0, t1));
+            const double lo_t = fmin(t0, t1), hi_t = fmax(t0, t1);
+            if (lo_t > a_in) { a_in = lo_t; ax_in = a; }
+            if (hi_t < a_out) { a_out = hi_t; ax_out = a; }
         } else {
             inv[a] = 0.0;
             if (!(src[a] > 0.0 && src[a] < hi)) return false;
@@ -49,14 +52,24 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
 
     int vs[3], cnt[3], sg[3];
     float a0[3], da[3];
+    bool grazing = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const double ir = 1.0 / res[a];
         const double gin = (src[a] + a_in * d[a]) * ir;
         const double gout = (src[a] + a_out * d[a]) * ir;
+        // nearly parallel to the planes of this axis and within reach of one:
+        // the reference's charge then depends on FP64 rounding of a clamped slope
+        if (d[a] != 0.0) {
+            const double glo = fmin(gin, gout), ghi = fmax(gin, gout);
+            if (ghi - glo < 1e-3 && floor(ghi + 1e-9) != floor(glo - 1e-9)) grazing = true;
+        }
         sg[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
-        int s0 = (int)floor(gin + sg[a] * 1e-6);
-        int e0 = (int)floor(gout - sg[a] * 1e-6);
+        // On the entry / exit face the voxel is known exactly; on the other axes
+        // the voxel is the floor of the coordinate, as the reference's
+        // midpoint-floor rule gives for lines along a grid plane.
+        int s0 = (a == ax_in) ? (sg[a] > 0 ? 0 : n[a] - 1) : (int)floor(gin);
+        int e0 = (a == ax_out) ? (sg[a] > 0 ? n[a] - 1 : 0) : (int)floor(gout);
         s0 = min(max(s0, 0), n[a] - 1);
         e0 = min(max(e0, 0), n[a] - 1);
         vs[a] = s0;
@@ -80,6 +93,7 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
     w.s2 = sg[2] * n[0] * n[1];
     w.idx = (vs[2] * n[1] + vs[1]) * n[0] + vs[0];
     w.nseg = 1 + cnt[0] + cnt[1] + cnt[2];
+    w.grazing = grazing;
     w.L = (float)(a_out - a_in);
     w.scale = (float)sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     return true;

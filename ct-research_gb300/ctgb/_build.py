@@ -21,7 +21,9 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libctgb.so"
 OBJDIR = LIBDIR / "obj"
 
-SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu"]
+SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu", "ref_walk.cu"]
+# ref_walk.cu replays the reference's FP64 walk operation by operation: no FMA contraction
+PER_FILE_FLAGS = {"ref_walk.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +57,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
     def one(src: str):
         obj = OBJDIR / (Path(src).stem + ".o")
-        cmd = [exe, *_flags(extra), "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [exe, *_flags(extra + PER_FILE_FLAGS.get(src, [])), "-c", str(CSRC / src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

@@ -38,6 +38,8 @@ SIGNATURES = {
     "ct_cone_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_bp_update": (_i, [_vp, _vp, _vp, _f, _f, _f, _f, _vp, _vp]),
     "ct_cone_fdk": (_i, [_vp, _vp, _vp, _vp]),
+    "ct_cone_fdk_filter": (_i, [_vp, _vp, _vp, _vp]),
+    "ct_cone_fdk_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_count_segments": (_i, [_vp, C.POINTER(_ll), _vp]),
     "ct_fan_plan_create": (_i, [C.POINTER(_vp), _i, _i, _vp, _vp, _i, _vp, _i, _d]),
     "ct_fan_plan_destroy": (_i, [_vp]),

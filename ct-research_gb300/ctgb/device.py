@@ -99,6 +99,18 @@ class ConePlan:
         _lib.call("ct_cone_fdk", self._h, _tptr(proj), _tptr(out), _stream())
         return out
 
+    def fdk_filter(self, proj: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Cosine pre-weight + S-L ramp of every detector row (FDK's first stage)."""
+        out = torch.empty_like(proj) if out is None else out
+        _lib.call("ct_cone_fdk_filter", self._h, _tptr(proj), _tptr(out), _stream())
+        return out
+
+    def fdk_bp(self, filtered: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """LR^2-weighted backprojection of a filtered sinogram (FDK's second stage)."""
+        out = self.new_volume(filtered.device) if out is None else out
+        _lib.call("ct_cone_fdk_bp", self._h, _tptr(filtered), _tptr(out), _stream())
+        return out
+
     def count_segments(self) -> int:
         n = C.c_longlong()
         _lib.call("ct_cone_count_segments", self._h, C.byref(n), _stream())

@@ -147,6 +147,11 @@ int ct_cone_bp_update(ct_cone_plan *plan, const float *d_proj, const float *d_co
                       float lambda, float lo, float hi, float *d_vol, void *stream);
 /* FDK reconstruction of d_proj into d_vol (modes from ct_cone_plan_set_fdk_mode). */
 int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream);
+/* The two FDK stages on their own: cosine pre-weight + S-L ramp into
+ * d_filtered (sinogram layout), and the LR^2-weighted backprojection of an
+ * already filtered sinogram. */
+int ct_cone_fdk_filter(ct_cone_plan *plan, const float *d_proj, float *d_filtered, void *stream);
+int ct_cone_fdk_bp(ct_cone_plan *plan, const float *d_filtered, float *d_vol, void *stream);
 /* Exact number of Siddon segments over all rays of the plan (host result). */
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream);
 

@@ -896,12 +896,21 @@ OC_API long long oc_cone_segments(int nt, int ns, int nz, const double *res, dou
             if (amax < a_out) a_out = amax;
         }
         if (miss || a_out <= a_in) continue;
+        /* voxels traversed = 1 + plane crossings per axis; on the entry / exit
+           face the voxel is exact, elsewhere the floor of the coordinate */
         long long c = 1;
         for (int k = 0; k < 3; ++k) {
+            if (d[k] == 0.0) continue;
             double g0 = (src[k] + a_in * d[k]) / res[k], g1 = (src[k] + a_out * d[k]) / res[k];
-            double lo = g0 < g1 ? g0 : g1, hi = g0 < g1 ? g1 : g0;
-            long long cnt = (long long)ceil(hi) - (long long)floor(lo) - 1;
-            if (cnt > 0) c += cnt;
+            double lo_k = fmin((0 - src[k]) / d[k], (n[k] * res[k] - src[k]) / d[k]);
+            double hi_k = fmax((0 - src[k]) / d[k], (n[k] * res[k] - src[k]) / d[k]);
+            long long s0 = (lo_k == a_in) ? (d[k] > 0 ? 0 : n[k] - 1) : (long long)floor(g0);
+            long long e0 = (hi_k == a_out) ? (d[k] > 0 ? n[k] - 1 : 0) : (long long)floor(g1);
+            if (s0 < 0) s0 = 0;
+            if (s0 > n[k] - 1) s0 = n[k] - 1;
+            if (e0 < 0) e0 = 0;
+            if (e0 > n[k] - 1) e0 = n[k] - 1;
+            c += s0 > e0 ? s0 - e0 : e0 - s0;
         }
         total += c;
     }
