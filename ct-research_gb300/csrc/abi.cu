@@ -105,16 +105,17 @@ using namespace ct;
 // ---------------------------------------------------------------------------
 struct ct_cone_plan {
     ConeGeom g{};
-    DevBuf trig, P, xi;
-    DevBuf quads, rcov, G, wtab, norms, graze;
+    DevBuf trig, vsrc, P, xi;
+    DevBuf quads, rcov, G, wtab, norms, graze, volT;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     // host copies of the geometry (drop-in cache key)
     std::vector<float> hb, hp, hx;
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
-        trig.release(); P.release(); xi.release();
+        trig.release(); vsrc.release(); P.release(); xi.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
+        volT.release();
     }
 };
 
@@ -170,12 +171,19 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     // the reference evaluates sin/cos of the float angle with the
     // single-precision overloads (ProjectionCone_3D.cu:26-28)
     std::vector<double2> tr(nb);
-    for (int v = 0; v < nb; ++v) tr[v] = make_double2((double)sinf(beta[v]), (double)cosf(beta[v]));
-    if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->P, P, np)) || (s = upload(pl->xi, xi, nx))) {
+    std::vector<ViewSrc> vs(nb);
+    for (int v = 0; v < nb; ++v) {
+        const double sb = (double)sinf(beta[v]), cb = (double)cosf(beta[v]);
+        tr[v] = make_double2(sb, cb);
+        vs[v] = ViewSrc{Size[0] / 2 - D * sb, Size[1] / 2 + D * cb, D * sb, D * cb};
+    }
+    if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->vsrc, vs.data(), nb)) || (s = upload(pl->P, P, np)) ||
+        (s = upload(pl->xi, xi, nx))) {
         delete pl;
         return s;
     }
     g.trig = pl->trig.as<double2>();
+    g.vsrc = pl->vsrc.as<ViewSrc>();
     g.P = pl->P.as<float>();
     g.xi = pl->xi.as<float>();
     pl->hb.assign(beta, beta + nb);
@@ -203,24 +211,36 @@ int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode) 
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
     return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
-           plan->graze.bytes;
+           plan->graze.bytes + plan->volT.bytes;
+}
+
+// The [z][t][s] copy of the volume the forward projector reads for views
+// whose detector rows run along s (plan workspace, refreshed every call).
+static int transposed_copy(ct_cone_plan *plan, const float *d_vol, float **volT, cudaStream_t st) {
+    const size_t n = (size_t)plan->g.nt * plan->g.ns * plan->g.nz;
+    int s = plan->volT.ensure(n * sizeof(float));
+    if (s) return s;
+    *volT = plan->volT.as<float>();
+    return cone_transpose_ts(plan->g, d_vol, *volT, st);
 }
 
 int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stream) {
     CT_REQUIRE(plan && d_vol && d_proj, "ct_cone_fp: null argument");
     GrazeList gl;
-    int s = graze_list(plan->graze, gl);
-    if (s) return s;
-    return cone_fp_launch(plan->g, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl, as_stream(stream));
+    float *volT;
+    int s;
+    if ((s = graze_list(plan->graze, gl)) || (s = transposed_copy(plan, d_vol, &volT, as_stream(stream)))) return s;
+    return cone_fp_launch(plan->g, d_vol, volT, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl, as_stream(stream));
 }
 
 int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b, const float *d_rowsum,
                         float eps, float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(plan && d_vol && d_b && d_out && d_norms, "ct_cone_fp_residual: null argument");
     GrazeList gl;
-    int s = graze_list(plan->graze, gl);
-    if (s) return s;
-    return cone_fp_launch(plan->g, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
+    float *volT;
+    int s;
+    if ((s = graze_list(plan->graze, gl)) || (s = transposed_copy(plan, d_vol, &volT, as_stream(stream)))) return s;
+    return cone_fp_launch(plan->g, d_vol, volT, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
 static int cone_bp_common(ct_cone_plan *plan, const float *d_proj, float *d_vol, int weighting,
@@ -306,7 +326,8 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
     if (s) return s;
     CT_CUDA(cudaMemsetAsync(plan->norms.ptr, 0, 2 * sizeof(double), st), "memset");
     GrazeList gl{};
-    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, gl, st)))
+    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, gl,
+                            st)))
         return s;
     double h = 0;
     CT_CUDA(cudaMemcpyAsync(&h, plan->norms.ptr, sizeof(double), cudaMemcpyDeviceToHost, st), "copy");

@@ -27,9 +27,15 @@ namespace ct {
 
 namespace {
 
-constexpr int BP_BX = 32;   // t per block
-constexpr int BP_BY = 4;    // s per block
-constexpr int BP_ZC = 16;   // z per thread
+#ifndef CT_BP_ZC
+#define CT_BP_ZC 32
+#endif
+#ifndef CT_BP_MINB
+#define CT_BP_MINB 3
+#endif
+constexpr int BP_BX = 32;          // t per block
+constexpr int BP_BY = 4;           // s per block
+constexpr int BP_ZC = CT_BP_ZC;    // z per thread (register accumulators)
 
 __global__ void __launch_bounds__(256)
 pack_quads_kernel(const float *__restrict__ R, float4 *__restrict__ Q, int nb, int nx, int np) {
@@ -107,8 +113,32 @@ __device__ __noinline__ bool chord_entry_found(const ConeGeom &g, int ti, int si
     return zlo_t >= tlo && zlo_t <= thi && zlo_s >= slo && zlo_s <= shi;
 }
 
+// Last z of a column that a view reaches when the source->centre line passes
+// near a voxel edge (two faces' chord parameters tie within FP32 margins): the
+// reference's FP64 face tests may then all fail at some z, and it returns,
+// dropping that z and all above it for this view.  Called rarely (symmetric
+// geometries); kept out of line so the hot loop keeps its registers.
+__device__ __noinline__ int chord_end_z(const ConeGeom &g, int ti, int si, double sb, double cb, int zlo, int zhi,
+                                        bool tie_ts, float ztie, bool tz1, float zc1, bool tz2, float zc2) {
+    const float rz = (float)g.res[2];
+    const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);
+    int zab = 0x7fffffff;
+    if (tie_ts) {
+        // t/s faces limit the chord where |iz| <= ztie: check those z in order
+        for (int z = max(zlo, 0); z <= min(zhi, g.nz - 1); ++z) {
+            const float iz = fmaf((float)z, rz, x_base);
+            if (fabsf(iz) > ztie * (1.0f + 1e-5f)) continue;
+            if (!chord_entry_found(g, ti, si, z, sb, cb)) { zab = z; break; }
+        }
+    }
+    const int r1 = (int)rintf(zc1), r2 = (int)rintf(zc2);
+    if (tz1 && r1 >= zlo && r1 <= zhi && r1 < zab && !chord_entry_found(g, ti, si, r1, sb, cb)) zab = r1;
+    if (tz2 && r2 >= zlo && r2 <= zhi && r2 < zab && !chord_entry_found(g, ti, si, r2, sb, cb)) zab = r2;
+    return min(zhi, zab - 1);
+}
+
 template <int WMODE, bool UPDATE>
-__global__ void __launch_bounds__(BP_BX * BP_BY)
+__global__ void __launch_bounds__(BP_BX * BP_BY, CT_BP_MINB)
 cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict__ vol,
                const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
     // detector-row coordinate pairs (xi[x], xi[x+1]) for the interpolation weights
@@ -127,42 +157,43 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
     const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
     const float D = (float)g.D;
     const float ipint = 1.0f / g.pint, ixint = 1.0f / g.xint;
-
-    float acc[BP_ZC];
-    float zg[BP_ZC], zq[BP_ZC];   // per z: h_z / |iz| and iz^2 (chord weight)
-#pragma unroll
-    for (int k = 0; k < BP_ZC; ++k) {
-        acc[k] = 0.0f;
-        const float iz = (float)((z0 + k + 0.5) * g.res[2] - 0.5 * g.size[2]);
-        zg[k] = 0.5f * rz / fabsf(iz);
-        zq[k] = iz * iz;
-    }
     const float ht = 0.5f * (float)g.res[0], hs = 0.5f * (float)g.res[1], hz = 0.5f * rz;
     const float czf = (float)(0.5 * g.size[2]);
     const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);   // iz at z = 0
+    const float iz0 = fmaf((float)z0, rz, x_base);                    // iz of this thread's first z
+    // largest |iz| of the thread's z range: decides whether z faces can limit the chord
+    const float izmax = fmaxf(fabsf(iz0), fabsf(fmaf((float)(BP_ZC - 1), rz, iz0)));
+    const float iz_vol = fabsf(x_base);   // largest |iz| of the volume
+    const float irz = 1.0f / rz, iD = 1.0f / D;
     const long long vstride = (long long)g.nx * g.np;
+    const float x0s = g.x0, ixs = ixint;
+
+    float acc[BP_ZC];
+#pragma unroll
+    for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
 
     for (int v = 0; v < g.nb; ++v) {
         const double2 tr = g.trig[v];
         const float sb = (float)tr.x, cb = (float)tr.y;
         const float dect_t = fmaf(it, cb, is * sb);
         const float dect_s = fmaf(is, cb, -it * sb);
-        const float lr = D / (D - dect_s);
+        const float lr = D * __frcp_rn(D - dect_s);
         const float P = dect_t * lr;
         bool pin = P >= g.minp && P < g.maxp;
-        // xi(z) = (x_base + z rz) * lr; detector rows in range for z in [zlo, zhi]
-        const float xslope = rz * lr, xoff = x_base * lr;
-        const float zlo_f = (g.minx - xoff) / xslope, zhi_f = (g.maxx - xoff) / xslope;
+        // xi(z) = iz(z) * lr; detector rows in range for z in [zlo, zhi]
+        // xi(z) >= minx  <=>  z >= (minx / lr - x_base) / rz, with 1/lr = (D - dect_s) / D
+        const float ilr = (D - dect_s) * iD;
+        const float zlo_f = fmaf(g.minx, ilr, -x_base) * irz, zhi_f = fmaf(g.maxx, ilr, -x_base) * irz;
         int zlo = (int)ceilf(zlo_f);             // first z with xi >= minx
         int zhi = (int)ceilf(zhi_f) - 1;         // last z with xi < maxx
-        // FP32 rounding is ~1e-4 in z units and ~3e-5 mm in P: re-decide in FP64 near an edge
-        const bool near_edge = fabsf(zlo_f - rintf(zlo_f)) < 1e-3f || fabsf(zhi_f - rintf(zhi_f)) < 1e-3f ||
-                               fabsf(P - g.minp) < 1e-3f || fabsf(P - g.maxp) < 1e-3f;
+        // FP32 rounding is ~3e-5 in z units and ~2e-5 mm in P: re-decide in FP64 near an edge
+        const bool near_edge = fabsf(zlo_f - rintf(zlo_f)) < 2.5e-4f || fabsf(zhi_f - rintf(zhi_f)) < 2.5e-4f ||
+                               fabsf(P - g.minp) < 2e-4f || fabsf(P - g.maxp) < 2e-4f;
         if (near_edge) range_fp64(g, ti, si, tr.x, tr.y, pin, zlo, zhi);
         if (!pin) continue;   // whole column off the detector for this view
         if (WMODE == W_FDK_STICKY && zhi < zlo) continue;
-        // detector column: index as floor(|P - P0| / PInt), weights from the
-        // domain values (Backprojection3D.cu:73-83)
+        // detector column: index floor(|P - P0| / PInt), weights from the domain
+        // values (Backprojection3D.cu:73-83)
         int p1 = (int)(fabsf(P - g.p0) * ipint);
         p1 = min(max(p1, 0), g.np - 2);
         const float wq1 = fabsf(P - __ldg(g.P + p1)) * ipint;        // weight of column p1+1
@@ -170,56 +201,63 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         const float4 *Qv = Q + (long long)v * vstride + p1;
 
         float wv = 1.0f, mts = 0.0f, qq = 0.0f;
-        int zab = 0x7fffffff;   // first z dropped by the reference's early return
+        int zend = zhi;           // last z that receives this view's value
+        bool zlimit = false;      // some z face limits a chord in this thread's range
         if (WMODE == W_CHORD) {
             const float dt = it + D * sb, ds = is - D * cb;
-            const float mt = ht / fabsf(dt), ms = hs / fabsf(ds);
+            const float mt = ht * __frcp_rn(fabsf(dt)), ms = hs * __frcp_rn(fabsf(ds));
             mts = fminf(mt, ms);
             qq = fmaf(dt, dt, ds * ds);
+            zlimit = izmax * mts > hz;
             // The source->centre line passes near a voxel edge when two faces'
             // parameters tie; only then can the reference's FP64 face tests all
-            // fail.  Detect ties in FP32 with a wide margin, decide in FP64.
+            // fail and end the column.  Ties are found in FP32 with a wide margin
+            // and decided in FP64 (chord_end_z).  A z face can tie only where
+            // |iz| reaches hz / mts, i.e. when the volume is tall enough.
             const bool tie_ts = fabsf(mt - ms) <= 1e-5f * mts;
-            const float ztie = hz / mts;   // |iz| where the z faces tie with mts
-            const float zc1 = (czf + ztie) / rz - 0.5f, zc2 = (czf - ztie) / rz - 0.5f;
-            const float r1 = rintf(zc1), r2 = rintf(zc2);
-            const bool tz1 = fabsf(zc1 - r1) < 1e-3f && r1 >= (float)zlo && r1 <= (float)zhi;
-            const bool tz2 = fabsf(zc2 - r2) < 1e-3f && r2 >= (float)zlo && r2 <= (float)zhi;
-            if (tie_ts) {
-                // t/s faces limit the chord where |iz| <= ztie: check those z in order
-                for (int z = max(zlo, 0); z <= min(zhi, g.nz - 1); ++z) {
-                    const float iz = fmaf((float)z, rz, x_base);
-                    if (fabsf(iz) > ztie * (1.0f + 1e-5f)) continue;
-                    if (!chord_entry_found(g, ti, si, z, tr.x, tr.y)) { zab = z; break; }
-                }
+            bool tz1 = false, tz2 = false;
+            float zc1 = 0.0f, zc2 = 0.0f;
+            if (iz_vol * mts > 0.999f * hz) {
+                const float ztie = hz * __frcp_rn(mts);   // |iz| where the z faces tie with mts
+                zc1 = (czf + ztie) * irz - 0.5f;
+                zc2 = (czf - ztie) * irz - 0.5f;
+                tz1 = fabsf(zc1 - rintf(zc1)) < 1e-3f;
+                tz2 = fabsf(zc2 - rintf(zc2)) < 1e-3f;
             }
-            if (tz1 && (int)r1 < zab && !chord_entry_found(g, ti, si, (int)r1, tr.x, tr.y)) zab = (int)r1;
-            if (tz2 && (int)r2 < zab && !chord_entry_found(g, ti, si, (int)r2, tr.x, tr.y)) zab = (int)r2;
+            if (tie_ts || tz1 || tz2)
+                zend = chord_end_z(g, ti, si, tr.x, tr.y, zlo, zhi, tie_ts, hz / mts, tz1, zc1, tz2, zc2);
         } else {
             wv = lr * lr * g.bint;
         }
+        const float c0 = 2.0f * mts;
 #pragma unroll
         for (int k = 0; k < BP_ZC; ++k) {
             int z = z0 + k;
-            bool in = (z >= zlo) && (z <= zhi);
+            bool in = (z >= zlo) && (z <= zend);
+            float iz = fmaf((float)k, rz, iz0);
             if (WMODE == W_FDK_STICKY) {
                 in = z >= zlo;
-                z = min(z, zhi);
+                if (z > zhi) {
+                    z = zhi;
+                    iz = fmaf((float)zhi, rz, x_base);
+                }
             }
-            if (WMODE == W_CHORD) in = in && (z < zab);
-            const float xi = fmaf((float)z, xslope, xoff);
-            int x1 = (int)(fabsf(xi - g.x0) * ixint);
+            const float xi = iz * lr;
+            int x1 = (int)(fabsf(xi - x0s) * ixs);
             x1 = min(max(x1, 0), g.nx - 2);
             const float2 xd = xpair[x1];
             const float wx1 = fabsf(xi - xd.x) * ixint;     // weight of row x1+1
             const float wx0 = fabsf(xd.y - xi) * ixint;     // weight of row x1
-            const float4 q = __ldg(Qv + (long long)x1 * g.np);
+            const float4 q = __ldg(Qv + x1 * g.np);
             const float top = fmaf(wq0, q.x, wq1 * q.y);
             const float bot = fmaf(wq0, q.z, wq1 * q.w);
             const float val = fmaf(wx0, top, wx1 * bot);
             float w;
             if (WMODE == W_CHORD) {
-                w = 2.0f * fminf(mts, zg[k]) * sqrtf(qq + zq[k]);
+                // chord 2 * min(h_a / |d_a|) * |d|, d = (dt, ds, iz)
+                const float d2 = fmaf(iz, iz, qq);
+                const float len = d2 * rsqrtf(d2);
+                w = zlimit ? 2.0f * fminf(mts, hz / fabsf(iz)) * len : c0 * len;
             } else {
                 w = wv;
             }

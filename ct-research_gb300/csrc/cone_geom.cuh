@@ -4,6 +4,11 @@
 
 namespace ct {
 
+// Per-view source position and the D sin / D cos terms of the ray direction, FP64.
+struct __align__(16) ViewSrc {
+    double src_t, src_s, dsb, dcb;
+};
+
 // Geometry of one cone scan in the reference's conventions
 // (ProjectionCone_3D.cpp:5-22, Backprojection3D.cu:20-27).
 struct ConeGeom {
@@ -13,6 +18,7 @@ struct ConeGeom {
     double res[3];           // voxel pitch Size/length
     double D;                // source to rotation centre
     const double2 *trig;     // per view (sin beta, cos beta), float-overload values widened
+    const ViewSrc *vsrc;     // per view source and D sin / D cos, FP64
     const float *P;          // detector column coordinates
     const float *xi;         // detector row coordinates
     // detector sampling as the reference derives it (Backprojection3D.cu:304-311)
