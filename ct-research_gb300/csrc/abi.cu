@@ -155,6 +155,7 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     g.res[0] = 1.0 * Size[0] / nt;
     g.res[1] = 1.0 * Size[1] / ns;
     g.res[2] = 1.0 * Size[2] / nz;
+    for (int a = 0; a < 3; ++a) g.ires[a] = 1.0 / g.res[a];
     g.D = D;
     // float-range bookkeeping of BackPro / FDKpro (Backprojection3D.cu:304-311)
     g.pint = np > 1 ? std::fabs(P[1] - P[0]) : 1.0f;
@@ -545,7 +546,10 @@ int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaS
                              Xigamadomain, LXigama, Distance);
     if (s) return s;
     // keep the exact resolution the caller passed
-    for (int a = 0; a < 3; ++a) pl->g.res[a] = resolution[a];
+    for (int a = 0; a < 3; ++a) {
+        pl->g.res[a] = resolution[a];
+        pl->g.ires[a] = 1.0 / resolution[a];
+    }
     DropinState &st = dropin();
     const size_t nv = (size_t)t_length * s_length * z_length, npj = (size_t)LBeta * LP * LXigama;
     if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;

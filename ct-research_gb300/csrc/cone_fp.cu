@@ -41,25 +41,27 @@ __device__ __forceinline__ double drcp1(double x) {
 __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x, bool tr_layout, RayWalk &w) {
     const ViewSrc vs = g.vsrc[v];
     const double2 tr = g.trig[v];
-    const double Pd = (double)g.P[p];
+    const float Pf = g.P[p], Xf = g.xi[x];
+    const double Pd = (double)Pf;
     const double src[3] = {vs.src_t, vs.src_s, 0.5 * g.size[2]};
-    const double d[3] = {fma(Pd, tr.y, vs.dsb), fma(Pd, tr.x, -vs.dcb), (double)g.xi[x]};
+    const double d[3] = {fma(Pd, tr.y, vs.dsb), fma(Pd, tr.x, -vs.dcb), (double)Xf};
     const int n[3] = {g.nt, g.ns, g.nz};
-    // FP32 slab test
-    float tin[3], tout[3];
+    // FP32 slab test on FP32 inputs: picks the entry and exit faces
+    const float srcf[3] = {(float)vs.src_t, (float)vs.src_s, (float)src[2]};
+    const float df[3] = {fmaf(Pf, (float)tr.y, (float)vs.dsb), fmaf(Pf, (float)tr.x, -(float)vs.dcb), Xf};
+    float tin[3], tout[3], idf[3];
     int ax_in = -1, ax_out = -1;
     float fin = -3.0e38f, fout = 3.0e38f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float hi = (float)(n[a] * g.res[a]);
-        const float sf = (float)src[a], df = (float)d[a];
-        if (df != 0.0f) {
-            const float inv = __frcp_rn(df);
-            const float t0 = (0.0f - sf) * inv, t1 = (hi - sf) * inv;
+        idf[a] = __frcp_rn(df[a]);
+        if (df[a] != 0.0f) {
+            const float t0 = (0.0f - srcf[a]) * idf[a], t1 = (hi - srcf[a]) * idf[a];
             tin[a] = fminf(t0, t1);
             tout[a] = fmaxf(t0, t1);
         } else {
-            if (!(sf > 0.0f && sf < hi)) return false;
+            if (!(srcf[a] > 0.0f && srcf[a] < hi)) return false;
             tin[a] = -3.0e38f;
             tout[a] = 3.0e38f;
         }
@@ -68,8 +70,8 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
     }
     // clear misses end here; near-tangent rays are decided by the FP64 test below
     if (ax_in < 0 || ax_out < 0 || !(fout >= fin - 1e-5f * fabsf(fin))) return false;
-    // FP64 entry / exit parameters from the faces the FP32 test chose; any other
-    // face within FP32 rounding of them is evaluated in FP64 too
+    // FP64 entry / exit parameters on the chosen faces; any other face within
+    // FP32 rounding of them is evaluated in FP64 too
     double a_in = -1.0e300, a_out = 1.0e300;
     const int ax_in32 = ax_in, ax_out32 = ax_out;
 #pragma unroll
@@ -80,10 +82,16 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
         if (!(cand_in || cand_out)) continue;
         const double inv = drcp1(d[a]);
         const double hi = n[a] * g.res[a];
-        const double t_lo = (0.0 - src[a]) * inv, t_hi = (hi - src[a]) * inv;
-        const double tn = fmin(t_lo, t_hi), tx = fmax(t_lo, t_hi);
-        if (cand_in && tn > a_in) { a_in = tn; ax_in = a; }
-        if (cand_out && tx < a_out) { a_out = tx; ax_out = a; }
+        const bool pos = d[a] > 0.0;
+        // a line going up enters at 0 and leaves at hi; going down the reverse
+        if (cand_in) {
+            const double t = ((pos ? 0.0 : hi) - src[a]) * inv;
+            if (t > a_in) { a_in = t; ax_in = a; }
+        }
+        if (cand_out) {
+            const double t = ((pos ? hi : 0.0) - src[a]) * inv;
+            if (t < a_out) { a_out = t; ax_out = a; }
+        }
     }
     if (!(a_out > a_in)) return false;
     const float L = (float)(a_out - a_in);
@@ -93,11 +101,12 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         sg[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
-        const double ir = 1.0 / g.res[a];
         // entry coordinate in voxel units: exact on the entry face, FP64 elsewhere
-        const double gin = (a == ax_in) ? (sg[a] > 0 ? 0.0 : (double)n[a]) : fma(a_in, d[a], src[a]) * ir;
-        const float stepf = (float)(g.res[a] / fabs(d[a]));       // parameter per plane
-        const float gout = (float)gin + L * (float)(d[a] * ir);    // exit coordinate, FP32
+        const double gin = (a == ax_in) ? (sg[a] > 0 ? 0.0 : (double)n[a]) : fma(a_in, d[a], src[a]) * g.ires[a];
+        const float ginf = (float)gin;
+        const float gstep = df[a] * (float)g.ires[a];               // voxel units per parameter unit
+        const float stepf = fabsf(__frcp_rn(gstep));                // parameter per plane
+        const float gout = fmaf(L, gstep, ginf);                    // exit coordinate, FP32
         int s0 = (a == ax_in) ? (sg[a] > 0 ? 0 : n[a] - 1) : (int)floor(gin);
         int e0 = (a == ax_out) ? (sg[a] > 0 ? n[a] - 1 : 0) : (int)floorf(gout);
         s0 = min(max(s0, 0), n[a] - 1);
@@ -105,12 +114,12 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
         vs0[a] = s0;
         cnt[a] = (sg[a] == 0) ? 0 : abs(e0 - s0);
         if (sg[a] != 0) {
-            const float glo = fminf((float)gin, gout), ghi = fmaxf((float)gin, gout);
+            const float glo = fminf(ginf, gout), ghi = fmaxf(ginf, gout);
             if (ghi - glo < 1e-3f && floorf(ghi + 1e-6f) != floorf(glo - 1e-6f)) grazing = true;
         }
         if (cnt[a] > 0) {
-            const double k1 = (double)(s0 + (sg[a] > 0 ? 1 : 0));
-            a0[a] = (float)fabs(k1 - gin) * stepf;
+            const int k1 = s0 + (sg[a] > 0 ? 1 : 0);
+            a0[a] = (float)fabs((double)k1 - gin) * stepf;
             da[a] = stepf;
         } else {
             a0[a] = __int_as_float(0x7f800000);   // +inf: no crossing on this axis
@@ -135,8 +144,7 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
     w.nseg = 1 + cnt[0] + cnt[1] + cnt[2];
     w.grazing = grazing;
     w.L = L;
-    const float dxf = (float)d[0], dyf = (float)d[1], dzf = (float)d[2];
-    w.scale = sqrtf(fmaf(dxf, dxf, fmaf(dyf, dyf, dzf * dzf)));
+    w.scale = sqrtf(fmaf(df[0], df[0], fmaf(df[1], df[1], df[2] * df[2])));
     return true;
 }
 

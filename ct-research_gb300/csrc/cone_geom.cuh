@@ -16,6 +16,7 @@ struct ConeGeom {
     int nb, np, nx;          // views, detector columns (P), detector rows (xi)
     double size[3];          // volume extent in mm
     double res[3];           // voxel pitch Size/length
+    double ires[3];          // 1 / res
     double D;                // source to rotation centre
     const double2 *trig;     // per view (sin beta, cos beta), float-overload values widened
     const ViewSrc *vsrc;     // per view source and D sin / D cos, FP64

@@ -360,3 +360,47 @@ def ellipsoid_line_integral(src, dst, ellipsoids):
         if t1 > t0:
             total += A * (t1 - t0) * np.linalg.norm(d)
     return total
+
+
+# -- SIRT loop and TV flow restated with the oracle operators (FP64) ---------
+def tv_flow(x, iters, step, eps=1e-8, lo=0.0):
+    """Normalised isotropic TV gradient flow on a [nz][ny][nx] (or [ny][nx])
+    array in FP64: g = d/dx sum sqrt(|D+ x|^2 + eps^2) with forward differences
+    and Neumann boundaries, x <- max(x - step * g / rms(g), lo) per sub-step.
+    This is the 3D forward-difference form of the TV flow of tv.m:30-44 used by
+    the SIRT-TV loop."""
+    x = np.array(x, dtype=np.float64)
+    squeeze = x.ndim == 2
+    if squeeze:
+        x = x[None]
+    for _ in range(iters):
+        dx = np.zeros_like(x); dy = np.zeros_like(x); dz = np.zeros_like(x)
+        dx[:, :, :-1] = x[:, :, 1:] - x[:, :, :-1]
+        dy[:, :-1, :] = x[:, 1:, :] - x[:, :-1, :]
+        dz[:-1, :, :] = x[1:, :, :] - x[:-1, :, :]
+        inv = 1.0 / np.sqrt(dx * dx + dy * dy + dz * dz + eps * eps)
+        px, py, pz = dx * inv, dy * inv, dz * inv
+        g = -(px + py + pz)
+        g[:, :, 1:] += px[:, :, :-1]
+        g[:, 1:, :] += py[:, :-1, :]
+        g[1:, :, :] += pz[:-1, :, :]
+        ss = float(np.sum(g * g))
+        if ss > 0:
+            x = np.maximum(x - step * np.sqrt(x.size / ss) * g, lo)
+    return x[0] if squeeze else x
+
+
+def sirt_loop(fp, bp, b, x0, iters, lam, lo, hi, eps, tv=None):
+    """SIRT update of SIRT.m:123-131 / SIRT3D.m:78-82 with given operators:
+    x <- clamp(x + lam * BP((b - FP x) / (FP 1 + eps)) / (BP 1 + eps), lo, hi),
+    optionally followed by tv(x) each iteration.  FP64 arrays."""
+    b = np.asarray(b, np.float64)
+    x = np.array(x0, dtype=np.float64)
+    rowsum = np.asarray(fp(np.ones_like(x)), np.float64)
+    colsum = np.asarray(bp(np.ones_like(b)), np.float64)
+    for _ in range(iters):
+        e = (b - np.asarray(fp(x), np.float64)) / (rowsum + eps)
+        x = np.clip(x + lam * np.asarray(bp(e), np.float64) / (colsum + eps), lo, hi)
+        if tv is not None:
+            x = tv(x)
+    return x
