@@ -168,8 +168,10 @@ def test_sirt_tv_graph_replay_equals_eager():
     cfg = dict(iters=5, lam=1.0, eps=1e-9, tv_iters=4, tv_step=1e-3)
     eager = Sirt(plan, b, SirtConfig(**cfg)).run()
     graph = Sirt(plan, b, SirtConfig(use_graph=True, **cfg)).run()
-    assert torch.equal(eager.x, graph.x)
-    assert eager.residuals == graph.residuals
+    assert torch.equal(eager.x, graph.x)            # the image kernels are deterministic
+    # the residual norms are double atomics: summation order may differ in the last bit
+    for (i0, r0), (i1, r1) in zip(eager.residuals, graph.residuals):
+        assert i0 == i1 and abs(r0 - r1) <= 1e-12 * abs(r0)
 
 
 @pytest.mark.gpu
