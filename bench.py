@@ -324,6 +324,149 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_batched2d(args):
+    """64 uneven 2D fan slices (N 128..512, views 90..720, bins 256..1024, seed 4),
+    100 SIRT iterations per slice as one CUDA-graph launch with autotuned blocks."""
+    import torch
+    import ctgb
+    from ctgb import geometry, phantom
+    from ctgb.batch import FanBatch, BatchedSirt, autotune
+    ctgb.load()
+    geoms = geometry.config_batched_fan(64, seed=4)
+    batch = FanBatch(geoms)
+    imgs = [phantom.ellipses_2d(g.nt, g.ns, phantom.ellipse_params(10, seed=100 + k), device="cuda")
+            for k, g in enumerate(geoms)]
+    b = batch.fp(batch.pack_images(imgs))
+    tune = autotune(batch, b)
+    sirt = BatchedSirt(batch, b)
+    iters = 100
+    x = batch.fbp(b).clamp_(0.0, 1.0)
+    g, norms = sirt.capture(x, iters)
+    x0 = x.clone()
+    times = []
+    for _ in range(args.warmup + args.steps):
+        x.copy_(x0)
+        norms.zero_()
+        e0, e1 = _events()
+        e0.record()
+        g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = min(times[args.warmup:])
+    hist = BatchedSirt.history(norms)
+    rays = batch.n_rays
+    line = {"metric": "batched 2D fan SIRT: GRay/s of FP+BP iterations", "value": rays * iters / t / 1e9,
+            "unit": "GRay/s", "ms_per_launch": t * 1e3, "iterations": iters, "slices": len(geoms),
+            "rays_per_iteration": rays, "pixels": batch.n_img, "blocks": tune["blocks"],
+            "residual_first_last_median": [float(np.median(hist[0])), float(np.median(hist[-1]))],
+            "config": {"workload": "64 slices N~U{128..512}, views~U{90..720}, bins~U{256..1024}, seed 4; "
+                                   "FBPfan start, lam 2, x in [0,1]; one graph launch = 100 iterations"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_sirt_tv(args):
+    """SIRT3D + TV on the 512^3 / 360-view / 768x512 workload: Poisson noise at 1e5
+    photons/ray (seed 3), FDK start, lam 1, x >= 0, 20 TV sub-steps of 1e-3 per
+    iteration; time per iteration and the data residual."""
+    import torch
+    import ctgb
+    from ctgb import geometry, phantom
+    from ctgb.device import ConePlan, FDK_FILTER_CLEAN, FDK_BP_ZERO
+    from ctgb.sirt import Sirt, SirtConfig
+    ctgb.load()
+    geom = geometry.config_cone_512()
+    vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2), device="cuda")
+    plan = ConePlan(geom, fdk_filter=FDK_FILTER_CLEAN, fdk_bp=FDK_BP_ZERO)
+    clean = plan.fp(vol)
+    b, _ = phantom.poisson_noise(clean, 1e5, 4.0, seed=3)
+    x0 = plan.fdk(b).clamp_(min=0.0)
+    iters = args.iters
+    cfg = SirtConfig(iters=iters, lam=1.0, eps=1e-9, tv_iters=20, tv_step=1e-3, use_graph=True,
+                     check_every=max(1, iters // 10))
+    s = Sirt(plan, b, cfg)
+    res = s.run(x0.clone())
+    r_final = s.data_residual(res.x)
+    rel_err = float(torch.linalg.vector_norm(res.x - vol) / torch.linalg.vector_norm(vol))
+    line = {"metric": "SIRT3D-TV 512^3 s/iteration", "value": res.seconds / res.iterations, "unit": "s",
+            "iterations": res.iterations, "seconds": res.seconds, "final_relative_residual": r_final,
+            "residual_history": res.residuals, "rel_l2_vs_phantom": rel_err,
+            "fdk_rel_l2_vs_phantom": float(torch.linalg.vector_norm(x0 - vol) / torch.linalg.vector_norm(vol)),
+            "config": {"workload": "cone_512, Poisson 1e5, FDK start, 20 TV sub-steps/iter, graph replay"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_fdk(args):
+    """FDK of the 256^3 / 360-view / 512x384 cone scan (reference launch-order
+    filter and sticky backprojection)."""
+    import torch
+    import ctgb
+    from ctgb import geometry, phantom
+    from ctgb.device import ConePlan
+    ctgb.load()
+    geom = geometry.config_cone_fdk()
+    vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=1), device="cuda")
+    plan = ConePlan(geom)
+    proj = plan.fp(vol)
+    out = plan.new_volume()
+    filt = torch.empty_like(proj)
+    for _ in range(args.warmup):
+        plan.fdk(proj, out)
+    ts = []
+    for _ in range(args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        plan.fdk_filter(proj, filt)
+        e[1].record()
+        plan.fdk_bp(filt, out)
+        e[2].record()
+        torch.cuda.synchronize()
+        ts.append((e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])))
+    tf, tb = np.median([a for a, _ in ts]), np.median([b_ for _, b_ in ts])
+    V, B = geom.n_voxels, len(geom.beta)
+    line = {"metric": "FDK 256^3 ms", "value": float(tf + tb), "unit": "ms", "filter_ms": float(tf),
+            "bp_ms": float(tb), "bp_algorithmic_gbs": (16 * V * B + 8 * V) / (tb / 1e3) / 1e9,
+            "rel_l2_vs_phantom": float(torch.linalg.vector_norm(out - vol) / torch.linalg.vector_norm(vol)),
+            "config": {"workload": "cone_fdk_256: 256^3 over 128 mm, 360 views, 512x384, SID 600 / SDD 1200"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_fan2d(args):
+    """2D fan FP + FBPfan: 256^2, 360 views, 512 bins, source-iso 500 mm."""
+    import torch
+    import ctgb
+    from ctgb import geometry, phantom
+    from ctgb.device import FanPlan
+    ctgb.load()
+    geom = geometry.config_fan2d()
+    img = phantom.ellipses_2d(geom.nt, geom.ns, phantom.ellipse_params(10, seed=0), device="cuda")
+    plan = FanPlan(geom)
+    proj = plan.fp(img)
+    rec = plan.fbp(proj)
+    for _ in range(args.warmup):
+        plan.fp(img, proj)
+        plan.fbp(proj, rec)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    e[0].record()
+    for _ in range(args.steps):
+        plan.fp(img, proj)
+    e[1].record()
+    for _ in range(args.steps):
+        plan.fbp(proj, rec)
+    e[2].record()
+    torch.cuda.synchronize()
+    tfp, tfbp = e[0].elapsed_time(e[1]) / args.steps, e[1].elapsed_time(e[2]) / args.steps
+    line = {"metric": "2D fan FP + FBP ms", "value": tfp + tfbp, "unit": "ms", "fp_ms": tfp, "fbp_ms": tfbp,
+            "rays": int(np.prod(geom.sino_shape)),
+            "config": {"workload": "fan2d_256: 256^2, 360 views, 512 bins, D 500 mm"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,13 +477,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
     ap.add_argument("--size", choices=["full", "small"], default="full",
                     help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
+    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d"], default="pair",
+                    help="pair (default): the FP+BP throughput line; the others report their own metric")
+    ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "pair":
         run_ours(args)
+    else:
+        {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d}[args.workload](args)
 
 
 if __name__ == "__main__":

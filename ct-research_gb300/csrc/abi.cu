@@ -700,3 +700,149 @@ int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// batches of uneven 2D fan slices (fan_batch.cu)
+// ---------------------------------------------------------------------------
+struct ct_fan_batch {
+    std::vector<ct_fan_plan *> plans;
+    std::vector<BatchSlice> h;
+    DevBuf desc, graze;
+    int fp_block = 128, bp_block = 128;
+    int fp_blocks = 0, bp_blocks = 0;
+    long long img_total = 0, sino_total = 0;
+    ~ct_fan_batch() {
+        for (ct_fan_plan *p : plans) delete p;
+        desc.release();
+        graze.release();
+    }
+};
+
+// Offsets of every slice in the packed buffers and its first block in each grid.
+static int batch_layout(ct_fan_batch *b) {
+    long long io = 0, so = 0, fb = 0, bb = 0;
+    for (size_t k = 0; k < b->plans.size(); ++k) {
+        BatchSlice &s = b->h[k];
+        s.g = b->plans[k]->g;
+        s.img_off = io;
+        s.sino_off = so;
+        s.ray_blk0 = (int)fb;
+        s.pix_blk0 = (int)bb;
+        const long long nr = (long long)s.g.nb * s.g.np, npx = (long long)s.g.nt * s.g.ns;
+        io += npx;
+        so += nr;
+        fb += (nr + b->fp_block - 1) / b->fp_block;
+        bb += (npx + b->bp_block - 1) / b->bp_block;
+    }
+    CT_REQUIRE(fb < (1LL << 31) && bb < (1LL << 31), "batch too large for one launch");
+    b->img_total = io;
+    b->sino_total = so;
+    b->fp_blocks = (int)fb;
+    b->bp_blocks = (int)bb;
+    return upload(b->desc, b->h.data(), b->h.size());
+}
+
+extern "C" {
+
+int ct_fan_batch_create(ct_fan_batch **out, int nslices, const int *t_length, const int *s_length, const double *Size,
+                        const double *const *BetaScanRange, const int *LBeta, const double *const *Pdomain,
+                        const int *LP, const double *Distance) {
+    CT_REQUIRE(out && nslices > 0 && t_length && s_length && Size && BetaScanRange && LBeta && Pdomain && LP &&
+                   Distance,
+               "ct_fan_batch_create: null argument");
+    CT_REQUIRE(nslices < (1 << 23), "ct_fan_batch_create: too many slices");
+    *out = nullptr;
+    ct_fan_batch *b = new ct_fan_batch();
+    b->plans.assign(nslices, nullptr);
+    b->h.resize(nslices);
+    for (int k = 0; k < nslices; ++k) {
+        int s = LP[k] >= 2 ? ct_fan_plan_create(&b->plans[k], t_length[k], s_length[k], Size + 2 * k,
+                                                 BetaScanRange[k], LBeta[k], Pdomain[k], LP[k], Distance[k])
+                           : (set_error("ct_fan_batch_create: every slice needs at least 2 detector bins"), CT_ERR_ARG);
+        if (!s && (long long)LBeta[k] * LP[k] >= (1LL << 40)) {
+            set_error("ct_fan_batch_create: slice sinogram too large");
+            s = CT_ERR_ARG;
+        }
+        if (s) {
+            delete b;
+            return s;
+        }
+    }
+    int s = batch_layout(b);
+    if (s) {
+        delete b;
+        return s;
+    }
+    *out = b;
+    return CT_OK;
+}
+
+int ct_fan_batch_destroy(ct_fan_batch *batch) {
+    delete batch;
+    return CT_OK;
+}
+
+int ct_fan_batch_layout(const ct_fan_batch *b, long long *img_offsets, long long *sino_offsets) {
+    CT_REQUIRE(b && img_offsets && sino_offsets, "ct_fan_batch_layout: null argument");
+    const size_t n = b->h.size();
+    for (size_t k = 0; k < n; ++k) {
+        img_offsets[k] = b->h[k].img_off;
+        sino_offsets[k] = b->h[k].sino_off;
+    }
+    img_offsets[n] = b->img_total;
+    sino_offsets[n] = b->sino_total;
+    return CT_OK;
+}
+
+int ct_fan_batch_set_blocks(ct_fan_batch *b, int fp_block, int bp_block) {
+    CT_REQUIRE(b, "ct_fan_batch_set_blocks: null batch");
+    CT_REQUIRE(fp_block >= 32 && fp_block <= 512 && fp_block % 32 == 0 && bp_block >= 32 && bp_block <= 512 &&
+                   bp_block % 32 == 0,
+               "ct_fan_batch_set_blocks: block sizes must be multiples of 32 in [32, 512]");
+    b->fp_block = fp_block;
+    b->bp_block = bp_block;
+    return batch_layout(b);
+}
+
+int ct_fan_batch_fp(ct_fan_batch *b, const float *d_img, float *d_proj, void *stream) {
+    CT_REQUIRE(b && d_img && d_proj, "ct_fan_batch_fp: null argument");
+    GrazeList gl;
+    int s = graze_list(b->graze, gl);
+    if (s) return s;
+    return fan_batch_fp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->fp_blocks, b->fp_block, d_img, d_proj,
+                               nullptr, nullptr, 0.f, nullptr, 0, gl, as_stream(stream));
+}
+
+int ct_fan_batch_fp_residual(ct_fan_batch *b, const float *d_img, const float *d_b, const float *d_rowsum, float eps,
+                             float *d_out, double *d_norms, void *stream) {
+    CT_REQUIRE(b && d_img && d_b && d_out && d_norms, "ct_fan_batch_fp_residual: null argument");
+    GrazeList gl;
+    int s = graze_list(b->graze, gl);
+    if (s) return s;
+    return fan_batch_fp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->fp_blocks, b->fp_block, d_img, d_out,
+                               d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
+}
+
+int ct_fan_batch_bp(ct_fan_batch *b, const float *d_proj, float *d_img, void *stream) {
+    CT_REQUIRE(b && d_proj && d_img, "ct_fan_batch_bp: null argument");
+    return fan_batch_bp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->bp_blocks, b->bp_block, d_proj, d_img, 0,
+                               nullptr, 0.f, 0.f, 0.f, 0.f, false, as_stream(stream));
+}
+
+int ct_fan_batch_bp_update(ct_fan_batch *b, const float *d_proj, const float *d_colsum, float eps, float lambda,
+                           float lo, float hi, float *d_img, void *stream) {
+    CT_REQUIRE(b && d_proj && d_colsum && d_img, "ct_fan_batch_bp_update: null argument");
+    return fan_batch_bp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->bp_blocks, b->bp_block, d_proj, d_img, 0,
+                               d_colsum, eps, lambda, lo, hi, true, as_stream(stream));
+}
+
+int ct_fan_batch_fbp(ct_fan_batch *b, const float *d_proj, float *d_img, int filter_mode, void *stream) {
+    CT_REQUIRE(b && d_proj && d_img, "ct_fan_batch_fbp: null argument");
+    for (size_t k = 0; k < b->h.size(); ++k) {
+        int s = ct_fan_fbp(b->plans[k], d_proj + b->h[k].sino_off, d_img + b->h[k].img_off, filter_mode, stream);
+        if (s) return s;
+    }
+    return CT_OK;
+}
+
+}  // extern "C"

@@ -1,28 +1,10 @@
-// fan2d.cu -- 2D fan- and parallel-beam projectors and backprojectors.
-//
-// Forward projectors: one thread per ray, the Siddon walk of siddon.cuh on a
-// one-slice volume (n[2] = 1, no z crossings).
-//  * fan (ProjectionFan_2D.cu:19-216): source (C_t - D sin b, C_s + D cos b),
-//    ray through the point P on the line through the centre perpendicular to
-//    the central ray: d = (P cos b + D sin b, P sin b - D cos b).
-//  * parallel (ProjectionParallel_2D.cu:23-243): ray of offset t at angle th,
-//    direction (-sin th, cos th) in (x, y) = (width, height) coordinates,
-//    through (C_x + t cos th, C_y + t sin th).
-// Backprojectors: one thread per pixel with the view loop inside and the sum in
-// a register; written once (no atomics).
-//  * BACKPROJ (BackprojectionFan2D.cu:7-116): linear interpolation of R at the
-//    pixel's detector position P/U times the reference's weight
-//    2 * |T1S1 - End|: End is the far point 2*Rscan along the source->pixel
-//    line and T1S1 its crossing with the pixel's low t edge (accepted when the
-//    crossing's s lies in [0, s_high], as the reference tests) or else its low
-//    s edge (t in [0, t_high]); pixel-views with neither add nothing.
-//  * FBPFAN (FBPfan.cu:45-96): filtered R interpolated, times dbeta / U^2.
-//  * FBPPAR (FBPparallel.cu:41-89): filtered R at t = x cos th + y sin th, times dth.
-#include "kernels.cuh"
-#include "siddon.cuh"
+// fan2d.cu -- single-slice 2D fan- and parallel-beam projectors and
+// backprojectors (device code in fan2d_dev.cuh).  One thread per ray for the
+// forward projectors, one thread per pixel (all views, sum in a register,
+// written once) for the backprojectors.
+#include "fan2d_dev.cuh"
 
 namespace ct {
-
 
 namespace {
 
@@ -37,35 +19,11 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
     const bool active = r < (long long)g.nb * g.np;
     double r2 = 0.0, b2 = 0.0;
     if (active) {
-        const int p = (int)(r % g.np), v = (int)(r / g.np);
-        const double2 tr = g.trig_d[v];
-        const double sb = tr.x, cb = tr.y;
-        const double P = g.Pd[p];
-        double src[3], d[3];
-        const int n[3] = {g.nt, g.ns, 1};
-        double res[3] = {g.res[0], g.res[1], 1.0};
-        if (g.parallel) {
-            // x = width axis (t index), y = height axis (s index)
-            src[0] = 0.5 * g.size[0] + P * cb + g.smax * sb;
-            src[1] = 0.5 * g.size[1] + P * sb - g.smax * cb;
-            d[0] = -sb;
-            d[1] = cb;
-        } else {
-            src[0] = 0.5 * g.size[0] - g.D * sb;
-            src[1] = 0.5 * g.size[1] + g.D * cb;
-            d[0] = P * cb + g.D * sb;
-            d[1] = P * sb - g.D * cb;
-        }
-        src[2] = 0.5;
-        d[2] = 0.0;
-        RayWalk w;
-        float val = 0.0f;
-        if (siddon_setup(src, d, n, res, w)) {
-            val = ray_integral(w, img, g.nt * g.ns - 1);
-            if (w.grazing) {
-                const int slot = atomicAdd(gl.count, 1);
-                if (slot < gl.cap) gl.rays[slot] = (unsigned long long)r;
-            }
+        bool grazing;
+        const float val = fan_ray_value(g, img, r, grazing);
+        if (grazing) {
+            const int slot = atomicAdd(gl.count, 1);
+            if (slot < gl.cap) gl.rays[slot] = (unsigned long long)r;
         }
         if (MODE == 0) {
             out[r] = (OutT)val;
@@ -84,70 +42,13 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
     }
 }
 
-enum { BP2_BACKPROJ = 0, BP2_FBPFAN = 1, BP2_FBPPAR = 2 };
-
 template <int WMODE, bool UPDATE>
 __global__ void __launch_bounds__(F2_BLOCK)
 fan_bp_kernel(const FanGeom g, const float *__restrict__ R, float *__restrict__ img,
               const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
     const int i = blockIdx.x * F2_BLOCK + threadIdx.x;
     if (i >= g.nt * g.ns) return;
-    const int ti = i % g.nt, si = i / g.nt;
-    const float it = (float)((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
-    const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
-    const float Rs = (float)g.D;
-    const float ipint = 1.0f / g.pint;
-    // pixel edges and centre in world coordinates (BackprojectionFan2D.cu:82)
-    const float tlo = (float)(ti * g.res[0]), thi_ = (float)((ti + 1) * g.res[0]);
-    const float slo = (float)(si * g.res[1]), shi_ = (float)((si + 1) * g.res[1]);
-    const float ct_ = (float)(0.5 * g.size[0]), cs_ = (float)(0.5 * g.size[1]);
-    float acc = 0.0f;
-    for (int v = 0; v < g.nb; ++v) {
-        const float2 tr = g.trig_f[v];
-        const float sb = tr.x, cb = tr.y;
-        const float P = fmaf(it, cb, is * sb);
-        float Pd = P, u = 1.0f;
-        if (WMODE != BP2_FBPPAR) {
-            const float S = fmaf(is, cb, -it * sb);
-            u = (Rs - S) / Rs;
-            Pd = P / u;
-        }
-        float val = 0.0f;
-        if (Pd >= g.minp && Pd < g.maxp) {
-            // index floor(|P - P0| / PInt), weights from the domain values
-            // (BackprojectionFan2D.cu:44-53)
-            int p1 = (int)(fabsf(Pd - g.p0) * ipint);
-            p1 = min(max(p1, 0), g.np - 2);
-            const float w1 = fabsf(Pd - __ldg(g.Pf + p1)) * ipint;
-            const float w0 = fabsf(__ldg(g.Pf + p1 + 1) - Pd) * ipint;
-            const float *Rv = R + (long long)v * g.np + p1;
-            val = fmaf(w0, __ldg(Rv), w1 * __ldg(Rv + 1));
-        }
-        if (WMODE == BP2_BACKPROJ) {
-            // unit direction of the source->detector-point line and its far end
-            const float ex0 = fmaf(Pd, cb, Rs * sb), ey0 = fmaf(Pd, sb, -Rs * cb);
-            const float inv = rsqrtf(fmaf(ex0, ex0, ey0 * ey0));
-            const float ex = ex0 * inv, ey = ey0 * inv;
-            const float st = ct_ - Rs * sb, ss = cs_ + Rs * cb;
-            const float a_end = 2.0f * Rs;
-            float a;
-            const float at = (tlo - st) / ex;
-            const float s_at = fmaf(at, ey, ss);
-            if (s_at >= 0.0f && s_at <= shi_) {
-                a = at;
-            } else {
-                const float as = (slo - ss) / ey;
-                const float t_as = fmaf(as, ex, st);
-                if (t_as >= 0.0f && t_as <= thi_) a = as;
-                else continue;
-            }
-            acc = fmaf(val, 2.0f * fabsf(a_end - a), acc);
-        } else if (WMODE == BP2_FBPFAN) {
-            acc += val / (u * u) * g.bint;
-        } else {
-            acc += val * g.bint;
-        }
-    }
+    const float acc = fan_pixel_sum<WMODE>(g, R, i);
     if (UPDATE) {
         const float x = img[i] + lambda * acc / (colsum[i] + eps);
         img[i] = fminf(fmaxf(x, lo), hi);

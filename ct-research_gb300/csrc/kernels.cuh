@@ -65,3 +65,24 @@ int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int n
 int sq_diff_sum_launch(const float *a, const float *b, long long n, double *out, cudaStream_t st);
 
 }  // namespace ct
+
+namespace ct {
+
+// One slice of a batch of uneven 2D fan scans (fan_batch.cu).
+struct BatchSlice {
+    FanGeom g;
+    long long img_off, sino_off;   // offsets into the packed image / sinogram buffers
+    int ray_blk0, pix_blk0;        // first block of the slice in the FP / BP grids
+};
+
+int fan_batch_fp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block, const float *img, float *out,
+                        const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
+                        cudaStream_t st);
+int fan_batch_bp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block, const float *R, float *img, int wmode,
+                        const float *colsum, float eps, float lambda, float lo, float hi, bool update,
+                        cudaStream_t st);
+int fan_batch_fixup_launch(const BatchSlice *d_sl, const float *img, float *out, const float *b, const float *rowsum,
+                           float eps, double *norms, int mode, const unsigned long long *list, const int *count,
+                           int cap, cudaStream_t st);
+
+}  // namespace ct

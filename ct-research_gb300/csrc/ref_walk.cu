@@ -261,7 +261,42 @@ fan_fixup_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restric
     }
 }
 
+// Batched slices: entries are (slice << 40) | ray.
+__global__ void __launch_bounds__(64)
+fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, const float *__restrict__ img, float *__restrict__ out,
+                       const float *__restrict__ b, const float *__restrict__ rowsum, float eps, double *norms, int mode,
+                       const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
+    const int n = min(*count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int k = (int)(list[i] >> 40);
+        const unsigned long long r = list[i] & ((1ULL << 40) - 1);
+        const FanGeom g = sl[k].g;
+        const int p = (int)(r % g.np), v = (int)(r / g.np);
+        const double2 tr = g.trig_d[v];
+        const float *im = img + sl[k].img_off;
+        const double val = g.parallel ? par_ray_ref(g, im, tr.x, tr.y, g.Pd[p]) : fan_ray_ref(g, im, tr.x, tr.y, g.Pd[p]);
+        const long long o = sl[k].sino_off + (long long)r;
+        if (mode == 0) {
+            out[o] = (float)val;
+        } else {
+            const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
+            const float r_old = rowsum ? out[o] * (rowsum[o] + eps) : out[o];
+            const float rr = b[o] - (float)val;
+            out[o] = rr * sc;
+            atomicAdd(norms + 2 * k, (double)rr * rr - (double)r_old * r_old);
+        }
+    }
+}
+
 }  // namespace
+
+int fan_batch_fixup_launch(const BatchSlice *d_sl, const float *img, float *out, const float *b, const float *rowsum,
+                           float eps, double *norms, int mode, const unsigned long long *list, const int *count,
+                           int cap, cudaStream_t st) {
+    fan_batch_fixup_kernel<<<64, 64, 0, st>>>(d_sl, img, out, b, rowsum, eps, norms, mode, list, count, cap);
+    CT_LAUNCH_CHECK("fan_batch_fixup_kernel");
+    return CT_OK;
+}
 
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
                       float eps, double *norms, int mode, const unsigned long long *list, const int *count, int cap,

@@ -48,6 +48,15 @@ SIGNATURES = {
     "ct_fan_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_fan_bp_update": (_i, [_vp, _vp, _vp, _f, _f, _f, _f, _vp, _vp]),
     "ct_fan_fbp": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "ct_fan_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ct_fan_batch_destroy": (_i, [_vp]),
+    "ct_fan_batch_layout": (_i, [_vp, _vp, _vp]),
+    "ct_fan_batch_set_blocks": (_i, [_vp, _i, _i]),
+    "ct_fan_batch_fp": (_i, [_vp, _vp, _vp, _vp]),
+    "ct_fan_batch_fp_residual": (_i, [_vp, _vp, _vp, _vp, _f, _vp, _vp, _vp]),
+    "ct_fan_batch_bp": (_i, [_vp, _vp, _vp, _vp]),
+    "ct_fan_batch_bp_update": (_i, [_vp, _vp, _vp, _f, _f, _f, _f, _vp, _vp]),
+    "ct_fan_batch_fbp": (_i, [_vp, _vp, _vp, _i, _vp]),
     "ct_tv_flow": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _vp]),
     "ct_sq_diff_sum": (_i, [_vp, _vp, _ll, _vp, _vp]),
 }

@@ -169,6 +169,34 @@ int ct_fan_bp_update(ct_fan_plan *plan, const float *d_proj, const float *d_cols
 int ct_fan_fbp(ct_fan_plan *plan, const float *d_proj, float *d_img, int filter_mode, void *stream);
 
 /* ===================================================================== */
+/* Batches of uneven 2D fan slices: every operator runs all slices in one */
+/* launch.  Images and sinograms are packed back to back in two device    */
+/* buffers at the offsets ct_fan_batch_layout returns.                    */
+/* ===================================================================== */
+
+typedef struct ct_fan_batch ct_fan_batch;
+
+/* Slice k: image t_length[k] x s_length[k], extent Size[2k..2k+1], views
+ * BetaScanRange[k][0..LBeta[k]), bins Pdomain[k][0..LP[k]), Distance[k]. */
+int ct_fan_batch_create(ct_fan_batch **batch, int nslices, const int *t_length, const int *s_length,
+                        const double *Size, const double *const *BetaScanRange, const int *LBeta,
+                        const double *const *Pdomain, const int *LP, const double *Distance);
+int ct_fan_batch_destroy(ct_fan_batch *batch);
+/* Offsets (in floats) of each slice in the packed image / sinogram buffers;
+ * element nslices holds the totals.  Arrays of nslices + 1. */
+int ct_fan_batch_layout(const ct_fan_batch *batch, long long *img_offsets, long long *sino_offsets);
+/* Threads per block of the forward / back projection launches (tuning). */
+int ct_fan_batch_set_blocks(ct_fan_batch *batch, int fp_block, int bp_block);
+int ct_fan_batch_fp(ct_fan_batch *batch, const float *d_img, float *d_proj, void *stream);
+/* d_norms: 2 doubles per slice, (|b - A x|^2, |b|^2) added. */
+int ct_fan_batch_fp_residual(ct_fan_batch *batch, const float *d_img, const float *d_b, const float *d_rowsum,
+                             float eps, float *d_out, double *d_norms, void *stream);
+int ct_fan_batch_bp(ct_fan_batch *batch, const float *d_proj, float *d_img, void *stream);
+int ct_fan_batch_bp_update(ct_fan_batch *batch, const float *d_proj, const float *d_colsum, float eps,
+                           float lambda, float lo, float hi, float *d_img, void *stream);
+int ct_fan_batch_fbp(ct_fan_batch *batch, const float *d_proj, float *d_img, int filter_mode, void *stream);
+
+/* ===================================================================== */
 /* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */
 /* ===================================================================== */
 
