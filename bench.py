@@ -387,7 +387,7 @@ def run_sirt_tv(args):
     b, _ = phantom.poisson_noise(clean, 1e5, 4.0, seed=3)
     x0 = plan.fdk(b).clamp_(min=0.0)
     iters = args.iters
-    cfg = SirtConfig(iters=iters, lam=1.0, eps=1e-9, tv_iters=20, tv_step=1e-3, use_graph=True,
+    cfg = SirtConfig(iters=iters, lam=1.0, eps=1e-9, tv_iters=20, tv_step=1e-3, use_graph=True, min_rowsum=0.5 * min(geom.size[a] / n for a, n in enumerate((geom.nt, geom.ns, geom.nz))), min_colsum_frac=0.05,
                      check_every=max(1, iters // 10))
     s = Sirt(plan, b, cfg)
     res = s.run(x0.clone())

@@ -32,7 +32,7 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
             const float rr = bb - val;
             const float sc = rowsum ? 1.0f / (rowsum[r] + eps) : 1.0f;
             out[r] = (OutT)(rr * sc);
-            r2 = (double)rr * rr;
+            r2 = grazing ? 0.0 : (double)rr * rr;   // grazing rays: added by the FP64 re-walk
             b2 = (double)bb * bb;
         }
     }

@@ -58,7 +58,7 @@ fan_batch_fp_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__r
             const float rr = bb - val;
             const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
             out[o] = rr * sc;
-            r2 = (double)rr * rr;
+            r2 = grazing ? 0.0 : (double)rr * rr;   // grazing rays: added by the FP64 re-walk
             b2 = (double)bb * bb;
         }
     }

@@ -85,19 +85,22 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
                 // summed as an unevaluated pair (s + c) with the TwoSum error-free
                 // transformation (Knuth), flushed into a double every 256 taps.
                 double dacc = 0.0;
-                float sh = 0.0f, sl = 0.0f;
                 const float *gp = G + (np - 1) + p;
-                int n = 0;
-                for (int q = g0; q < g1; ++q) {
-                    const float prod = __fmul_rn(mix[q], gp[-q]);
-                    const float t = __fadd_rn(sh, prod);
-                    const float bp = __fsub_rn(t, sh);
-                    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(prod, bp));
-                    sh = t;
-                    sl = __fadd_rn(sl, err);
-                    if (++n == 256) { dacc += (double)sh + (double)sl; sh = sl = 0.0f; n = 0; }
+                // chunks of 256 taps keep the double flush out of the inner loop
+                for (int q0 = g0; q0 < g1; q0 += 256) {
+                    const int q1 = min(q0 + 256, g1);
+                    float sh = 0.0f, sl = 0.0f;
+#pragma unroll 4
+                    for (int q = q0; q < q1; ++q) {
+                        const float prod = __fmul_rn(mix[q], gp[-q]);
+                        const float t = __fadd_rn(sh, prod);
+                        const float bp = __fsub_rn(t, sh);
+                        const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(prod, bp));
+                        sh = t;
+                        sl = __fadd_rn(sl, err);
+                    }
+                    dacc += (double)sh + (double)sl;
                 }
-                dacc += (double)sh + (double)sl;
                 o[p] = (float)((double)o[p] + (double)f.pint * dacc);
             }
             __syncthreads();
@@ -114,7 +117,9 @@ int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream
     if (smem > 48 * 1024)
         CT_CUDA(cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "row_filter smem attribute");
-    row_filter_kernel<<<f.nrow, FT, smem, st>>>(f, R, out);
+    // launch order: one thread per output of a P-tile, so no thread idles at the tile barriers
+    const int block = (f.launch_order && f.w) ? std::min(FT, std::max(32, (f.tile + 31) / 32 * 32)) : FT;
+    row_filter_kernel<<<f.nrow, block, smem, st>>>(f, R, out);
     CT_LAUNCH_CHECK("row_filter_kernel");
     return CT_OK;
 }

@@ -230,10 +230,9 @@ cone_fixup_kernel(const ConeGeom g, const float *__restrict__ vol, float *__rest
             out[r] = val;
         } else {
             const float sc = rowsum ? 1.0f / (rowsum[r] + eps) : 1.0f;
-            const float r_old = rowsum ? out[r] * (rowsum[r] + eps) : out[r];
             const float rr = b[r] - val;
             out[r] = rr * sc;
-            atomicAdd(norms, (double)rr * rr - (double)r_old * r_old);
+            atomicAdd(norms, (double)rr * rr);   // the fast kernel left this ray out of the norm
         }
     }
 }
@@ -253,10 +252,9 @@ fan_fixup_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restric
             out[r] = (OutT)val;
         } else {
             const float sc = rowsum ? 1.0f / (rowsum[r] + eps) : 1.0f;
-            const float r_old = rowsum ? (float)out[r] * (rowsum[r] + eps) : (float)out[r];
             const float rr = b[r] - (float)val;
             out[r] = (OutT)(rr * sc);
-            atomicAdd(norms, (double)rr * rr - (double)r_old * r_old);
+            atomicAdd(norms, (double)rr * rr);   // the fast kernel left this ray out of the norm
         }
     }
 }
@@ -280,10 +278,9 @@ fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, const float *__restric
             out[o] = (float)val;
         } else {
             const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
-            const float r_old = rowsum ? out[o] * (rowsum[o] + eps) : out[o];
             const float rr = b[o] - (float)val;
             out[o] = rr * sc;
-            atomicAdd(norms + 2 * k, (double)rr * rr - (double)r_old * r_old);
+            atomicAdd(norms + 2 * k, (double)rr * rr);   // left out by the fast kernel
         }
     }
 }

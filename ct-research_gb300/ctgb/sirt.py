@@ -50,6 +50,13 @@ class SirtConfig:
     use_graph: bool = False      # replay the iteration from a captured CUDA graph
     checkpoint: str | None = None
     checkpoint_every: int = 0
+    # Rays whose path through the volume is shorter than min_rowsum (mm) and
+    # voxels whose colsum is below min_colsum_frac * max(colsum) take no part
+    # in the update.  0 keeps every ray and voxel, as the reference does; with
+    # noisy data a corner-clipping ray has a tiny rowsum, and dividing its
+    # noise by it drives the unmatched voxel-driven A^T to diverge.
+    min_rowsum: float = 0.0
+    min_colsum_frac: float = 0.0
 
 
 @dataclass
@@ -74,6 +81,11 @@ class Sirt:
         ones_b = torch.ones_like(b)
         self.rowsum = plan.fp(ones_x)
         self.colsum = plan.bp(ones_b)
+        # an infinite normaliser makes 1 / (sum + eps) exactly 0: the ray / voxel drops out
+        if cfg.min_rowsum > 0:
+            self.rowsum[self.rowsum < cfg.min_rowsum] = float("inf")
+        if cfg.min_colsum_frac > 0:
+            self.colsum[self.colsum < cfg.min_colsum_frac * float(self.colsum.max())] = float("inf")
         self.e = torch.empty_like(b)
         self.norms = torch.zeros(2, dtype=torch.float64, device=b.device)
         self.tv_work = torch.empty_like(ones_x) if cfg.tv_iters > 0 else None
