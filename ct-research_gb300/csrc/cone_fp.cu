@@ -185,7 +185,7 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
                 const float r = bb - val;
                 const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
                 out[o] = r * sc;
-                r2 = w.grazing ? 0.0 : (double)r * r;   // grazing rays: added by the FP64 re-walk
+                r2 = (hit && w.grazing) ? 0.0 : (double)r * r;   // grazing rays: added by the FP64 re-walk
                 b2 = (double)bb * bb;
             }
         }
