@@ -29,6 +29,7 @@ SIGNATURES = {
     "ct_BackprojectionFan2D": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _d]),
     "ct_FBPfan": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _d]),
     "ct_FBPpara": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _i, _i]),
+    "ct_FBPfan_noalloc": (_i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _i, _i, _d, _vp]),
     "ct_cone_plan_create": (_i, [C.POINTER(_vp), _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _i, _d]),
     "ct_cone_plan_destroy": (_i, [_vp]),
     "ct_cone_plan_set_fdk_mode": (_i, [_vp, _i, _i]),

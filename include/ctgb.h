@@ -102,6 +102,19 @@ int ct_FBPfan(float *Display, const float *R, const float *Pdomain, const float 
 int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float *ThetaScanRange,
                int LTheta, int LT, const double *Size, int t_length, int s_length);
 
+/* 2D fan FBP (as ct_FBPfan) that allocates no device memory; no counterpart in
+ * the reference.  For callers that may not call cudaMalloc / cudaFree while they
+ * run (memory reserved once at start-up, or a framework-owned device pool).
+ * d_R (LBeta x LP sinogram) and d_Display (t x s image) are device buffers of the
+ * caller; Pdomain, BetaScanRange and Size are host arrays.  All other data sits
+ * in one library-owned 8 MiB device array: sizes that do not fit return
+ * CT_ERR_ARG.  The first call on a device looks up that array's address; make it
+ * before any stream capture.  Calls share the array, so calls that overlap on the
+ * GPU race: serialise them.  Work is queued on `stream` (cudaStream_t). */
+int ct_FBPfan_noalloc(float *d_Display, const float *d_R, const float *Pdomain,
+                      const float *BetaScanRange, int LBeta, int LP, const double *Size, int t_length,
+                      int s_length, double Rscan, void *stream);
+
 /* ===================================================================== */
 /* Plans and device-pointer entry points (data stays in HBM).             */
 /* ===================================================================== */
