@@ -79,21 +79,118 @@ static int graze_list(DevBuf &b, GrazeList &gl) {
     return CT_OK;
 }
 
-// Shepp-Logan-form taps exactly as GFunction computes them (FDK.cu:6-19):
-// double arithmetic, stored as float.
-static std::vector<float> sl_taps(float pint, int np) {
-    const double PI = 3.141592653589793;
+constexpr double kPi = 3.141592653589793;
+
+// Ramp filter taps (2*np-1, centre np-1), computed in double, stored as float.
+//  CT_FILTER_SHEPP_LOGAN: exactly as GFunction computes them (FDK.cu:6-19).
+//  CT_FILTER_RAM_LAK: the kernel of FBP_parallel.m:241-251 (h[0] = 1/(2 dP)^2,
+//    0 at even n, -1/(n pi dP)^2 at odd n) times 1/2, the amplitude convention
+//    of the Shepp-Logan taps (whose centre is half the textbook 2/(pi dP)^2),
+//    so that switching the filter keeps the image scale.
+static std::vector<float> ramp_taps(int kind, float pint, int np) {
     std::vector<float> g(2 * (size_t)np - 1);
     for (int n = 0; n < np; ++n) {
-        if (n == 0) {
-            g[np - 1] = (float)(1.0 / (1.0 * (PI * pint) * (PI * pint)));
+        double v;
+        if (kind == CT_FILTER_RAM_LAK) {
+            if (n == 0) {
+                v = 0.5 / ((2.0 * pint) * (2.0 * pint));
+            } else if (n % 2 == 0) {
+                v = 0.0;
+            } else {
+                const double a = (double)n * kPi * pint;
+                v = -0.5 / (a * a);
+            }
+        } else if (n == 0) {
+            v = 1.0 / (1.0 * (kPi * pint) * (kPi * pint));
         } else {
-            const double a = 1.0 * ((double)pint * PI) * ((double)pint * PI);
-            const double v = -1.0 / a / (4 * (1.0 * n * n) - 1);
-            g[np - 1 - n] = g[np - 1 + n] = (float)v;
+            const double a = 1.0 * ((double)pint * kPi) * ((double)pint * kPi);
+            v = -1.0 / a / (4 * (1.0 * n * n) - 1);
         }
+        g[np - 1 - n] = g[np - 1 + n] = (float)v;
     }
     return g;
+}
+
+// Symmetric Hamming window of m taps, 0.54 - 0.46 cos(2 pi k / (m - 1)), the
+// smoothing window of the commented post-filter in FanProjection.m:265-270.
+static std::vector<double> hamming(int m) {
+    std::vector<double> h(m, 1.0);
+    if (m > 1)
+        for (int k = 0; k < m; ++k) h[k] = 0.54 - 0.46 * std::cos(2.0 * kPi * k / (m - 1));
+    return h;
+}
+
+// Short-scan weight of ParkFunction.m:6-16 for the ray at fan angle gama of the
+// view at beta (radians); b0 is the first view angle, fan the full fan angle.
+// The two ramps use beta itself, not beta - b0, as ParkFunction.m:9,13 do.
+static double parker(double beta, double b0, double gama, double fan) {
+    if (beta >= b0 && beta < b0 + fan - 2 * gama) {
+        const double s = std::sin(kPi / 4 * beta / (fan / 2 - gama));
+        return s * s;
+    }
+    if (beta >= b0 + fan - 2 * gama && beta <= b0 + kPi - 2 * gama) return 1.0;
+    if (beta > b0 + kPi - 2 * gama && beta <= b0 + kPi + fan) {
+        const double s = std::sin(kPi / 4 * (kPi + fan - beta) / (fan / 2 + gama));
+        return s * s;
+    }
+    return 0.0;
+}
+
+// Short-scan weights per (view, bin), gama = atan(P / D) on the flat detector
+// at the isocentre.  Each weight is doubled: a short scan covers each line
+// once, and the half-amplitude ramp taps assume the double coverage of a full
+// turn (FanProjection.m:280-288 doubles its taps for the same reason).
+static std::vector<float> parker_table(const std::vector<float> &beta, const std::vector<float> &P, double D) {
+    const int nb = (int)beta.size(), np = (int)P.size();
+    const double fan = std::fabs(std::atan((double)P[np - 1] / D) - std::atan((double)P[0] / D));
+    std::vector<float> w((size_t)nb * np);
+    for (int v = 0; v < nb; ++v)
+        for (int p = 0; p < np; ++p)
+            w[(size_t)v * np + p] = (float)(2.0 * parker(beta[v], beta[0], std::atan((double)P[p] / D), fan));
+    return w;
+}
+
+// Filter-stage options of a plan (ct_*_plan_set_filter / _set_short_scan).
+struct FilterOpts {
+    int kind = CT_FILTER_SHEPP_LOGAN;
+    int wlen = 0;
+    int short_scan = 0;
+};
+
+// Device tables of the filter options: the taps always, the short-scan
+// weights and the smoothing window when they are switched on.
+static int filter_tables(const FilterOpts &o, float pint, int np, const std::vector<float> &beta,
+                         const std::vector<float> &P, double D, DevBuf &G, DevBuf &pwt, DevBuf &win,
+                         double &wsum) {
+    int s;
+    std::vector<float> taps = ramp_taps(o.kind, pint, np);
+    if ((s = upload(G, taps.data(), taps.size()))) return s;
+    if (o.short_scan) {
+        std::vector<float> w = parker_table(beta, P, D);
+        if ((s = upload(pwt, w.data(), w.size()))) return s;
+    }
+    if (o.wlen > 0) {
+        std::vector<double> h = hamming(o.wlen);
+        wsum = 0.0;
+        for (double x : h) wsum += x;
+        if ((s = upload(win, h.data(), h.size()))) return s;
+    }
+    return CT_OK;
+}
+
+static void filter_fields(const FilterOpts &o, int rows_per_view, const DevBuf &pwt, const DevBuf &win, double wsum,
+                          RowFilter &f) {
+    f.pw = o.short_scan ? pwt.as<float>() : nullptr;
+    f.pw_div = rows_per_view;
+    f.win = o.wlen > 0 ? win.as<double>() : nullptr;
+    f.wlen = o.wlen;
+    f.wsum = wsum;
+}
+
+static int check_filter_opts(int kind, int window_len) {
+    CT_REQUIRE(kind == CT_FILTER_SHEPP_LOGAN || kind == CT_FILTER_RAM_LAK, "filter kind must be CT_FILTER_*");
+    CT_REQUIRE(window_len >= 0 && window_len <= 1024, "window length must be in [0, 1024]");
+    return CT_OK;
 }
 
 }  // namespace ct
@@ -106,16 +203,18 @@ using namespace ct;
 struct ct_cone_plan {
     ConeGeom g{};
     DevBuf trig, vsrc, P, xi;
-    DevBuf quads, rcov, G, wtab, norms, graze, volT;
+    DevBuf quads, rcov, G, wtab, norms, graze, volT, pwt, win;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
+    FilterOpts filt;
+    double wsum = 0.0;
     // host copies of the geometry (drop-in cache key)
     std::vector<float> hb, hp, hx;
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
         trig.release(); vsrc.release(); P.release(); xi.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
-        volT.release();
+        volT.release(); pwt.release(); win.release();
     }
 };
 
@@ -209,6 +308,24 @@ int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode) 
     return CT_OK;
 }
 
+int ct_cone_plan_set_filter(ct_cone_plan *plan, int kind, int window_len) {
+    CT_REQUIRE(plan, "plan is null");
+    int s = check_filter_opts(kind, window_len);
+    if (s) return s;
+    plan->filt.kind = kind;
+    plan->filt.wlen = window_len;
+    plan->G.release();   // tables are rebuilt on the next filter call
+    return CT_OK;
+}
+
+int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable) {
+    CT_REQUIRE(plan, "plan is null");
+    CT_REQUIRE(enable == 0 || enable == 1, "enable must be 0 or 1");
+    plan->filt.short_scan = enable;
+    plan->G.release();
+    return CT_OK;
+}
+
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
     return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
@@ -272,8 +389,9 @@ static int cone_fdk_filter_into(ct_cone_plan *plan, const float *d_proj, float *
     CT_REQUIRE(g.np >= 2 && g.nx >= 2, "FDK: detector needs at least 2x2 samples");
     int s;
     if (!plan->G.ptr) {
-        std::vector<float> taps = sl_taps(g.pint, g.np);
-        if ((s = upload(plan->G, taps.data(), taps.size()))) return s;
+        if ((s = filter_tables(plan->filt, g.pint, g.np, plan->hb, plan->hp, g.D, plan->G, plan->pwt, plan->win,
+                               plan->wsum)))
+            return s;
         // pre-weight D / sqrt(D^2 + P^2 + xi^2) per (xi, P), in double (FDK.cu:34)
         std::vector<double> w((size_t)g.nx * g.np);
         for (int x = 0; x < g.nx; ++x)
@@ -295,6 +413,7 @@ static int cone_fdk_filter_into(ct_cone_plan *plan, const float *d_proj, float *
     f.limit = 2048;      // FDK.h:24 Filterlengthlimit
     f.row_block = 256;   // FDK.h:23 blockX
     f.rowmod = g.nx;
+    filter_fields(plan->filt, g.nx, plan->pwt, plan->win, plan->wsum, f);
     return row_filter_launch(f, d_proj, d_out, st);
 }
 
@@ -344,11 +463,13 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
 // ---------------------------------------------------------------------------
 struct ct_fan_plan {
     FanGeom g{};
-    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze;
-    std::vector<float> hPf;
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze, pwt, win;
+    std::vector<float> hPf, hbf;
+    FilterOpts filt;
+    double wsum = 0.0;
     ~ct_fan_plan() {
         trig_d.release(); Pd.release(); trig_f.release(); Pf.release();
-        G.release(); wtab.release(); rcov.release(); graze.release();
+        G.release(); wtab.release(); rcov.release(); graze.release(); pwt.release(); win.release();
     }
 };
 
@@ -403,6 +524,7 @@ static int fan_plan_make(ct_fan_plan **out, int nt, int ns, const double size2[2
     g.trig_f = pl->trig_f.as<float2>();
     g.Pf = pl->Pf.as<float>();
     pl->hPf = pf;
+    pl->hbf = bf;
     *out = pl;
     return CT_OK;
 }
@@ -417,6 +539,25 @@ int ct_fan_plan_create(ct_fan_plan **plan, int nt, int ns, const double *Size, c
 
 int ct_fan_plan_destroy(ct_fan_plan *plan) {
     delete plan;
+    return CT_OK;
+}
+
+int ct_fan_plan_set_filter(ct_fan_plan *plan, int kind, int window_len) {
+    CT_REQUIRE(plan, "plan is null");
+    int s = check_filter_opts(kind, window_len);
+    if (s) return s;
+    plan->filt.kind = kind;
+    plan->filt.wlen = window_len;
+    plan->G.release();   // tables are rebuilt on the next filter call
+    return CT_OK;
+}
+
+int ct_fan_plan_set_short_scan(ct_fan_plan *plan, int enable) {
+    CT_REQUIRE(plan, "plan is null");
+    CT_REQUIRE(enable == 0 || enable == 1, "enable must be 0 or 1");
+    CT_REQUIRE(!plan->g.parallel, "short-scan weights need a fan geometry");
+    plan->filt.short_scan = enable;
+    plan->G.release();
     return CT_OK;
 }
 
@@ -457,8 +598,9 @@ int ct_fan_fbp(ct_fan_plan *plan, const float *d_proj, float *d_img, int filter_
     cudaStream_t st = as_stream(stream);
     int s;
     if (!plan->G.ptr) {
-        std::vector<float> taps = sl_taps(g.pint, g.np);
-        if ((s = upload(plan->G, taps.data(), taps.size()))) return s;
+        if ((s = filter_tables(plan->filt, g.pint, g.np, plan->hbf, plan->hPf, g.D, plan->G, plan->pwt, plan->win,
+                               plan->wsum)))
+            return s;
         if (!g.parallel) {
             std::vector<double> w(g.np);   // Rscan / sqrt(Rscan^2 + P^2) (FBPfan.cu:32)
             for (int p = 0; p < g.np; ++p) {
@@ -481,6 +623,7 @@ int ct_fan_fbp(ct_fan_plan *plan, const float *d_proj, float *d_img, int filter_
     f.limit = g.parallel ? 2048 : 1024;       // FBPparallel.h:26 / FBPfan.h:26
     f.row_block = g.parallel ? 256 : 128;
     f.rowmod = g.nb;
+    filter_fields(plan->filt, 1, plan->pwt, plan->win, plan->wsum, f);
     if ((s = row_filter_launch(f, d_proj, plan->rcov.as<float>(), st))) return s;
     return fan_bp_launch(g, plan->rcov.as<float>(), d_img, g.parallel ? 2 : 1, nullptr, 0.f, 0.f, 0.f, 0.f, false,
                          st);
@@ -802,6 +945,16 @@ int ct_fan_batch_set_blocks(ct_fan_batch *b, int fp_block, int bp_block) {
     b->fp_block = fp_block;
     b->bp_block = bp_block;
     return batch_layout(b);
+}
+
+int ct_fan_batch_set_filter(ct_fan_batch *b, int kind, int window_len, int short_scan) {
+    CT_REQUIRE(b, "ct_fan_batch_set_filter: null batch");
+    for (ct_fan_plan *p : b->plans) {
+        int s;
+        if ((s = ct_fan_plan_set_filter(p, kind, window_len)) || (s = ct_fan_plan_set_short_scan(p, short_scan)))
+            return s;
+    }
+    return CT_OK;
 }
 
 int ct_fan_batch_fp(ct_fan_batch *b, const float *d_img, float *d_proj, void *stream) {

@@ -13,6 +13,11 @@
 // so far, and later tiles unweighted; rows of the residual row tile launch
 // the residual P-tile first.  CLEAN mode weights the whole row once.
 //
+// Options beyond the reference's GPU path: other ramp taps (Ram-Lak) only
+// change G; short-scan (Parker) weights multiply the raw row as it is loaded,
+// as a caller weighting the sinogram before the call would; a Hamming
+// smoothing window runs over each finished filtered row.
+//
 // One block per row; the row, its mixed copy and the taps live in shared
 // memory.  Partial sums run in FP32 and are flushed into a double every 128
 // taps; each chunk result is added into the float output as the reference's
@@ -37,8 +42,9 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
     const float *in = R + (long long)row * np;
     float *o = out + (long long)row * np;
     const double *w = f.w ? f.w + (long long)(row % f.wrows) * np : nullptr;
+    const float *pw = f.pw ? f.pw + (long long)(row / f.pw_div) * np : nullptr;
     for (int q = threadIdx.x; q < np; q += blockDim.x) {
-        raw[q] = in[q];
+        raw[q] = pw ? __fmul_rn(in[q], pw[q]) : in[q];
         o[q] = 0.0f;
     }
     for (int q = threadIdx.x; q < 2 * np - 1; q += blockDim.x) G[q] = f.G[q];
@@ -104,6 +110,21 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
                 o[p] = (float)((double)o[p] + (double)f.pint * dacc);
             }
             __syncthreads();
+        }
+    }
+    if (f.win) {
+        // smoothing of the filtered row: o[p] = sum_i win[i] x[p + i - wlen/2] / wsum,
+        // x zero outside the row; sequential double sum without contraction
+        for (int q = threadIdx.x; q < np; q += blockDim.x) raw[q] = o[q];
+        __syncthreads();
+        const int c = f.wlen / 2;
+        for (int p = threadIdx.x; p < np; p += blockDim.x) {
+            double acc = 0.0;
+            for (int i = 0; i < f.wlen; ++i) {
+                const int k = p + i - c;
+                if (k >= 0 && k < np) acc = __dadd_rn(acc, __dmul_rn((double)raw[k], f.win[i]));
+            }
+            o[p] = (float)__ddiv_rn(acc, f.wsum);
         }
     }
 }

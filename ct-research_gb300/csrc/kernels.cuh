@@ -30,6 +30,11 @@ struct RowFilter {
     int wrows;               // weight row = row % wrows
     int launch_order;        // 0 clean, 1 reference launch order
     int tile, limit, row_block, rowmod;   // reference tiling
+    const float *pw;         // short-scan weights [view][np] multiplied into the raw row, or nullptr
+    int pw_div;              // view of a row = row / pw_div
+    const double *win;       // smoothing window of wlen taps applied to the filtered row, or nullptr
+    int wlen;
+    double wsum;             // sum of the window taps (the divisor)
 };
 
 // Rays that graze a grid plane, listed by the fast projectors for the FP64

@@ -33,6 +33,8 @@ SIGNATURES = {
     "ct_cone_plan_create": (_i, [C.POINTER(_vp), _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _i, _d]),
     "ct_cone_plan_destroy": (_i, [_vp]),
     "ct_cone_plan_set_fdk_mode": (_i, [_vp, _i, _i]),
+    "ct_cone_plan_set_filter": (_i, [_vp, _i, _i]),
+    "ct_cone_plan_set_short_scan": (_i, [_vp, _i]),
     "ct_cone_plan_workspace_bytes": (C.c_size_t, [_vp]),
     "ct_cone_fp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_fp_residual": (_i, [_vp, _vp, _vp, _vp, _f, _vp, _vp, _vp]),
@@ -44,6 +46,8 @@ SIGNATURES = {
     "ct_cone_count_segments": (_i, [_vp, C.POINTER(_ll), _vp]),
     "ct_fan_plan_create": (_i, [C.POINTER(_vp), _i, _i, _vp, _vp, _i, _vp, _i, _d]),
     "ct_fan_plan_destroy": (_i, [_vp]),
+    "ct_fan_plan_set_filter": (_i, [_vp, _i, _i]),
+    "ct_fan_plan_set_short_scan": (_i, [_vp, _i]),
     "ct_fan_fp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_fan_fp_residual": (_i, [_vp, _vp, _vp, _vp, _f, _vp, _vp, _vp]),
     "ct_fan_bp": (_i, [_vp, _vp, _vp, _vp]),
@@ -58,6 +62,7 @@ SIGNATURES = {
     "ct_fan_batch_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_fan_batch_bp_update": (_i, [_vp, _vp, _vp, _f, _f, _f, _f, _vp, _vp]),
     "ct_fan_batch_fbp": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "ct_fan_batch_set_filter": (_i, [_vp, _i, _i, _i]),
     "ct_tv_flow": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _vp]),
     "ct_sq_diff_sum": (_i, [_vp, _vp, _ll, _vp, _vp]),
 }

@@ -93,6 +93,12 @@ class FanBatch:
     def n_rays(self):
         return self.n_sino
 
+    def set_filter(self, kind="shepp-logan", window: int = 0, short_scan: bool = False):
+        """FBP filter options of every slice (FanPlan.set_filter)."""
+        from .device import filter_kind
+        _lib.call("ct_fan_batch_set_filter", self._h, filter_kind(kind), int(window), int(bool(short_scan)))
+        return self
+
     def set_blocks(self, fp_block: int, bp_block: int):
         _lib.call("ct_fan_batch_set_blocks", self._h, int(fp_block), int(bp_block))
         self.blocks = (int(fp_block), int(bp_block))

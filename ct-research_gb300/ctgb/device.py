@@ -16,6 +16,16 @@ from .geometry import ConeGeometry, FanGeometry
 
 FDK_FILTER_CLEAN, FDK_FILTER_LAUNCH_ORDER = 0, 1
 FDK_BP_ZERO, FDK_BP_STICKY = 0, 1
+FILTERS = {"shepp-logan": 0, "ram-lak": 1}
+
+
+def filter_kind(kind) -> int:
+    """CT_FILTER_* value of a filter name ("shepp-logan", "ram-lak") or int."""
+    if isinstance(kind, str):
+        if kind.lower() not in FILTERS:
+            raise ValueError(f"unknown filter {kind!r}; expected one of {sorted(FILTERS)}")
+        return FILTERS[kind.lower()]
+    return int(kind)
 
 
 def _np_ptr(a):
@@ -51,6 +61,13 @@ class ConePlan:
                   len(geom.xi), float(geom.D))
         _lib.call("ct_cone_plan_set_fdk_mode", self._h, int(fdk_filter), int(fdk_bp))
         self._norms = None
+
+    def set_filter(self, kind="shepp-logan", window: int = 0, short_scan: bool = False):
+        """FDK filter stage: ramp taps, Hamming smoothing window length (0 =
+        none) and short-scan (Parker) weights.  The defaults are the reference's."""
+        _lib.call("ct_cone_plan_set_filter", self._h, filter_kind(kind), int(window))
+        _lib.call("ct_cone_plan_set_short_scan", self._h, int(bool(short_scan)))
+        return self
 
     def close(self):
         if self._h:
@@ -130,6 +147,12 @@ class FanPlan:
         self._keep = (size, geom.beta, geom.P)
         _lib.call("ct_fan_plan_create", C.byref(self._h), geom.nt, geom.ns, _np_ptr(size), _np_ptr(geom.beta),
                   len(geom.beta), _np_ptr(geom.P), len(geom.P), float(geom.D))
+
+    def set_filter(self, kind="shepp-logan", window: int = 0, short_scan: bool = False):
+        """FBP filter stage options, as ConePlan.set_filter."""
+        _lib.call("ct_fan_plan_set_filter", self._h, filter_kind(kind), int(window))
+        _lib.call("ct_fan_plan_set_short_scan", self._h, int(bool(short_scan)))
+        return self
 
     def close(self):
         if self._h:

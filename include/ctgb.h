@@ -122,13 +122,20 @@ int ct_FBPfan_noalloc(float *d_Display, const float *d_R, const float *Pdomain,
 typedef struct ct_cone_plan ct_cone_plan;
 typedef struct ct_fan_plan ct_fan_plan;
 
-/* Behaviour switches of the plans.  CT_COMPAT reproduces the reference
- * exactly where it has data-dependent quirks; the default of every plan. */
+/* Behaviour switches of the plans.  Every plan starts with the settings that
+ * reproduce the reference exactly, data-dependent quirks included
+ * (LAUNCH_ORDER, STICKY, Shepp-Logan taps, no window, full scan). */
 enum {
     CT_FDK_FILTER_CLEAN = 0,       /* weight the whole row, then filter */
     CT_FDK_FILTER_LAUNCH_ORDER = 1,/* reference: in-place weight seen in launch order (FDK.cu:36-44) */
     CT_FDK_BP_ZERO = 0,            /* off-detector voxels add 0 */
     CT_FDK_BP_STICKY = 1           /* reference: they re-add the last in-range value (FDK.cu:73,100-123) */
+};
+
+/* Ramp filters of the FDK / FBP filter stage. */
+enum {
+    CT_FILTER_SHEPP_LOGAN = 0,     /* GFunction taps (FDK.cu:6-19), the reference's GPU filter */
+    CT_FILTER_RAM_LAK = 1          /* FBP_parallel.m:241-251, scaled by 1/2 to the Shepp-Logan amplitude */
 };
 
 /* Cone geometry; arrays are host pointers copied into the plan.  Angles,
@@ -141,6 +148,15 @@ int ct_cone_plan_create(ct_cone_plan **plan, int t_length, int s_length, int z_l
 int ct_cone_plan_destroy(ct_cone_plan *plan);
 /* FDK behaviour (CT_FDK_FILTER_*, CT_FDK_BP_*). Defaults: LAUNCH_ORDER, STICKY. */
 int ct_cone_plan_set_fdk_mode(ct_cone_plan *plan, int filter_mode, int bp_mode);
+/* Filter stage options; none has a counterpart in the reference's GPU code.
+ * kind: CT_FILTER_*.  window_len > 0 smooths every filtered row with a
+ * Hamming window of that many taps, out[p] = sum_i h[i] x[p + i - len/2] / sum(h)
+ * (the commented post-filter of FanProjection.m:265-270); 0 = none. */
+int ct_cone_plan_set_filter(ct_cone_plan *plan, int kind, int window_len);
+/* enable = 1: multiply the projections by 2x the short-scan weights of
+ * ParkFunction.m:6-16 (gama = atan(P / Distance), fan angle from the detector
+ * ends, start angle = BetaScanRange[0]) before the pre-weight and filter. */
+int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable);
 /* Device bytes of plan-owned workspace (packed sinogram, filter rows). */
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan);
 
@@ -173,6 +189,9 @@ int ct_fan_plan_create(ct_fan_plan **plan, int t_length, int s_length, const dou
                        const double *BetaScanRange, int LBeta, const double *Pdomain, int LP,
                        double Distance);
 int ct_fan_plan_destroy(ct_fan_plan *plan);
+/* FBP filter options, as ct_cone_plan_set_filter / ct_cone_plan_set_short_scan. */
+int ct_fan_plan_set_filter(ct_fan_plan *plan, int kind, int window_len);
+int ct_fan_plan_set_short_scan(ct_fan_plan *plan, int enable);
 int ct_fan_fp(ct_fan_plan *plan, const float *d_img, float *d_proj, void *stream);
 int ct_fan_fp_residual(ct_fan_plan *plan, const float *d_img, const float *d_b, const float *d_rowsum,
                        float eps, float *d_out, double *d_norms, void *stream);
@@ -208,6 +227,8 @@ int ct_fan_batch_bp(ct_fan_batch *batch, const float *d_proj, float *d_img, void
 int ct_fan_batch_bp_update(ct_fan_batch *batch, const float *d_proj, const float *d_colsum, float eps,
                            float lambda, float lo, float hi, float *d_img, void *stream);
 int ct_fan_batch_fbp(ct_fan_batch *batch, const float *d_proj, float *d_img, int filter_mode, void *stream);
+/* FBP filter options of every slice (ct_fan_plan_set_filter, ct_fan_plan_set_short_scan). */
+int ct_fan_batch_set_filter(ct_fan_batch *batch, int kind, int window_len, int short_scan);
 
 /* ===================================================================== */
 /* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */

@@ -319,77 +319,198 @@ OC_API void oc_fbpfan_weight_apply(float *out, const float *R, const float *P, i
             out[b * np + p] = (float)(R[b * np + p] * (rscan / sqrt(sq(rscan) + sq(P[p]))));
 }
 
-OC_API void oc_fdk_filter(float *rcov, const float *R, const float *xi, const float *P, int nb,
-                          int np, int nx, double D, int mode, int nthreads)
+/* Filter-stage options beyond the reference's GPU path.  NULL / 0 fields
+   give the reference's behaviour. */
+typedef struct {
+    const float *pw;      /* short-scan weights [view][np], or NULL */
+    int pw_div;           /* rows per view */
+    const double *win;    /* smoothing window, or NULL */
+    int wlen;
+    double wsum;
+} filt_opts;
+
+/* Pre-weight + ramp convolution of detector rows, shared by FDK and FBPfan.
+   mode 0 ("clean"): every output sees the fully pre-weighted row.
+   mode 1 ("launch order"): the reference weights the row in place inside the
+   kernel that convolves it, one P-tile per launch and `limit` taps per chunk
+   (FDK.cu:21-48 with the launch loops :333-477; FBPfan.cu:21-43 with
+   :286-420).  Model: a P-tile sees earlier tiles fully weighted, its own tile
+   weighted once per chunk processed so far, later tiles unweighted; rows of
+   the residual row tile (row % rowmod beyond the last full block of
+   row_block rows) run the residual P-tile first.
+   Options: short-scan weights multiply the raw row (float product) before any
+   of this; the smoothing window runs over the finished filtered row. */
+static void filter_rows(float *rcov, const float *R, long nrow, int np, float pint, const float *g,
+                        const double *wd, int wrows, int tile, int limit, int row_block, int rowmod,
+                        int mode, const filt_opts *o)
+{
+#pragma omp parallel
+    {
+        float *cur = (float *)malloc(sizeof(float) * np);
+        float *tmp = (float *)malloc(sizeof(float) * np);
+        int *pos = (int *)malloc(sizeof(int) * (np / tile + 2));
+#pragma omp for schedule(dynamic, 4)
+        for (long row = 0; row < nrow; ++row) {
+            const float *in = R + row * np;
+            const double *w = wd + (row % wrows) * np;
+            const float *pw = o->pw ? o->pw + (row / o->pw_div) * np : NULL;
+            float *out = rcov + row * np;
+            for (int p = 0; p < np; ++p) out[p] = 0.0f;
+            for (int p = 0; p < np; ++p) tmp[p] = pw ? in[p] * pw[p] : in[p];
+            int gtime = (int)ceil(1.0 * np / limit);
+            if (mode == 0) {
+                for (int p = 0; p < np; ++p) cur[p] = (float)(tmp[p] * w[p]);
+                for (int c = 0; c < gtime; ++c) {
+                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                    for (int p = 0; p < np; ++p) {
+                        double acc = 0;
+                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                        out[p] = (float)((double)out[p] + pint * acc);
+                    }
+                }
+            } else {
+                int nfull = np / tile, resid = np % tile, ntiles = nfull + (resid ? 1 : 0);
+                int ridx = (int)(row % rowmod);
+                int in_resid_rows = (rowmod % row_block) != 0 && ridx >= (rowmod / row_block) * row_block;
+                for (int k = 0; k < ntiles; ++k)
+                    pos[k] = (in_resid_rows && resid) ? ((k == nfull) ? 0 : k + 1) : k;
+                for (int p = 0; p < np; ++p) cur[p] = tmp[p];
+                for (int step = 0; step < ntiles; ++step) {
+                    int k = 0;
+                    for (int j = 0; j < ntiles; ++j) if (pos[j] == step) k = j;
+                    int p0 = k * tile, p1 = (k == nfull) ? np : p0 + tile;
+                    for (int c = 0; c < gtime; ++c) {
+                        for (int p = p0; p < p1; ++p) cur[p] = (float)(cur[p] * w[p]);
+                        int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
+                        for (int p = p0; p < p1; ++p) {
+                            double acc = 0;
+                            for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
+                            out[p] = (float)((double)out[p] + pint * acc);
+                        }
+                    }
+                }
+            }
+            if (o->win) {
+                /* out[p] = sum_i win[i] x[p + i - wlen/2] / wsum, x zero outside */
+                for (int p = 0; p < np; ++p) tmp[p] = out[p];
+                int c = o->wlen / 2;
+                for (int p = 0; p < np; ++p) {
+                    double acc = 0;
+                    for (int i = 0; i < o->wlen; ++i) {
+                        int k = p + i - c;
+                        if (k >= 0 && k < np) acc += (double)tmp[k] * o->win[i];
+                    }
+                    out[p] = (float)(acc / o->wsum);
+                }
+            }
+        }
+        free(cur);
+        free(tmp);
+        free(pos);
+    }
+}
+
+/* Ramp taps by kind: 0 Shepp-Logan (GFunction, as oc_sl_filter); 1 Ram-Lak,
+   the kernel of FBP_parallel.m:241-251 (h0 = 1/(2 dP)^2, even n 0, odd n
+   -1/(n pi dP)^2) times 1/2, the amplitude convention of the S-L taps. */
+OC_API void oc_ramp_taps(float *g, int kind, float pint, int np)
+{
+    if (kind != 1) { oc_sl_filter(g, pint, np); return; }
+    for (int n = 0; n < np; ++n) {
+        double v;
+        if (n == 0) v = 0.5 / ((2.0 * pint) * (2.0 * pint));
+        else if (n % 2 == 0) v = 0.0;
+        else { double a = (double)n * OC_PI * pint; v = -0.5 / (a * a); }
+        g[np - 1 - n] = (float)v;
+        g[np - 1 + n] = (float)v;
+    }
+}
+
+/* MATLAB hamming(m): 0.54 - 0.46 cos(2 pi k / (m - 1)), k = 0..m-1 (1 for m = 1). */
+OC_API void oc_hamming(double *h, int m)
+{
+    for (int k = 0; k < m; ++k) h[k] = (m > 1) ? 0.54 - 0.46 * cos(2.0 * OC_PI * k / (m - 1)) : 1.0;
+}
+
+/* ParkFunction.m:6-16 (beta, b0, gama in radians; fan = full fan angle). */
+static double park(double beta, double b0, double gama, double fan)
+{
+    if (beta >= b0 && beta < b0 + fan - 2 * gama) {
+        double s = sin(OC_PI / 4 * beta / (fan / 2 - gama));
+        return s * s;
+    } else if (beta >= b0 + fan - 2 * gama && beta <= b0 + OC_PI - 2 * gama) {
+        return 1.0;
+    } else if (beta > b0 + OC_PI - 2 * gama && beta <= b0 + OC_PI + fan) {
+        double s = sin(OC_PI / 4 * (OC_PI + fan - beta) / (fan / 2 + gama));
+        return s * s;
+    }
+    return 0.0;
+}
+
+/* 2 x ParkFunction weight per (view, bin): gama = atan(P / D), b0 = beta[0],
+   fan = |atan(P_last / D) - atan(P_0 / D)|; the factor 2 restores the full
+   amplitude of a once-covered line under the half-amplitude ramp taps. */
+OC_API void oc_parker_weights(float *pw, const float *beta, int nb, const float *P, int np, double D)
+{
+    double fan = fabs(atan((double)P[np - 1] / D) - atan((double)P[0] / D));
+    for (int v = 0; v < nb; ++v)
+        for (int p = 0; p < np; ++p)
+            pw[(long)v * np + p] = (float)(2.0 * park(beta[v], beta[0], atan((double)P[p] / D), fan));
+}
+
+static void make_opts(filt_opts *o, float **pwbuf, double **winbuf, const float *beta, int nb,
+                      const float *P, int np, double D, int rows_per_view, int wlen, int short_scan)
+{
+    memset(o, 0, sizeof(*o));
+    *pwbuf = NULL;
+    *winbuf = NULL;
+    if (short_scan) {
+        *pwbuf = (float *)malloc(sizeof(float) * (size_t)nb * np);
+        oc_parker_weights(*pwbuf, beta, nb, P, np, D);
+        o->pw = *pwbuf;
+        o->pw_div = rows_per_view;
+    }
+    if (wlen > 0) {
+        *winbuf = (double *)malloc(sizeof(double) * wlen);
+        oc_hamming(*winbuf, wlen);
+        double sum = 0;
+        for (int i = 0; i < wlen; ++i) sum += (*winbuf)[i];
+        o->win = *winbuf;
+        o->wlen = wlen;
+        o->wsum = sum;
+    }
+}
+
+/* FDK filter stage with options: taps kind, smoothing window, short scan. */
+OC_API void oc_fdk_filter_ex(float *rcov, const float *R, const float *xi, const float *P,
+                             const float *beta, int nb, int np, int nx, double D, int mode, int kind,
+                             int wlen, int short_scan, int nthreads)
 {
     set_threads(nthreads);
     det_range rg = make_range(P, np, xi, nx, NULL, 0);
     float *g = (float *)malloc(sizeof(float) * (2 * np - 1));
-    oc_sl_filter(g, rg.pint, np);
+    oc_ramp_taps(g, kind, rg.pint, np);
     /* the weight depends on (xi, P) only; the reference recomputes it per launch
        in double and multiplies in double, so keep it in double here */
     double *wd = (double *)malloc(sizeof(double) * (size_t)nx * np);
     for (int x = 0; x < nx; ++x)
         for (int p = 0; p < np; ++p)
             wd[(long)x * np + p] = D / sqrt(sq(D) + sq(P[p]) + sq(xi[x]));
-    /* mode 0 ("clean"): every output sees the fully pre-weighted row.
-       mode 1 ("launch order"): the reference weights the row in place inside
-       the kernel that convolves it, one P-tile of 256 samples per launch and
-       2048 taps per chunk (FDK.cu:21-48, launch loops :333-477).  Model: a
-       P-tile sees earlier tiles fully weighted, its own tile weighted once per
-       chunk processed so far, later tiles unweighted; rows of the residual
-       xi-tile run the residual P-tile first (:375-409 before :442-474). */
-#pragma omp parallel
-    {
-        float *cur = (float *)malloc(sizeof(float) * np);
-        int ntl = np / 256 + 2;
-        int *pos = (int *)malloc(sizeof(int) * ntl);
-#pragma omp for schedule(dynamic, 4)
-        for (long row = 0; row < (long)nb * nx; ++row) {
-            int x = (int)(row % nx);
-            const float *in = R + row * np;
-            const double *w = wd + (long)x * np;
-            float *out = rcov + row * np;
-            for (int p = 0; p < np; ++p) out[p] = 0.0f;
-            const int tile = 256, limit = 2048, row_block = 256;   /* FDK.h:22-24 */
-            int gtime = (int)ceil(1.0 * np / limit);
-            if (mode == 0) {
-                for (int p = 0; p < np; ++p) cur[p] = (float)(in[p] * w[p]);
-                for (int c = 0; c < gtime; ++c) {
-                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
-                    for (int p = 0; p < np; ++p) {
-                        double acc = 0;
-                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
-                        out[p] = (float)((double)out[p] + rg.pint * acc);
-                    }
-                }
-                continue;
-            }
-            int nfull = np / tile, resid = np % tile, ntiles = nfull + (resid ? 1 : 0);
-            int in_resid_rows = (nx % row_block) != 0 && x >= (nx / row_block) * row_block;
-            for (int k = 0; k < ntiles; ++k)
-                pos[k] = (in_resid_rows && resid) ? ((k == nfull) ? 0 : k + 1) : k;
-            for (int p = 0; p < np; ++p) cur[p] = in[p];
-            for (int step = 0; step < ntiles; ++step) {
-                int k = 0;
-                for (int j = 0; j < ntiles; ++j) if (pos[j] == step) k = j;
-                int p0 = k * tile, p1 = (k == nfull) ? np : p0 + tile;
-                for (int c = 0; c < gtime; ++c) {
-                    for (int p = p0; p < p1; ++p) cur[p] = (float)(cur[p] * w[p]);
-                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
-                    for (int p = p0; p < p1; ++p) {
-                        double acc = 0;
-                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
-                        out[p] = (float)((double)out[p] + rg.pint * acc);
-                    }
-                }
-            }
-        }
-        free(cur);
-        free(pos);
-    }
+    filt_opts o;
+    float *pwb;
+    double *winb;
+    make_opts(&o, &pwb, &winb, beta, nb, P, np, D, nx, wlen, short_scan);
+    filter_rows(rcov, R, (long)nb * nx, np, rg.pint, g, wd, nx, 256, 2048, 256, nx, mode, &o);  /* FDK.h:22-24 */
+    free(pwb);
+    free(winb);
     free(wd);
     free(g);
+}
+
+OC_API void oc_fdk_filter(float *rcov, const float *R, const float *xi, const float *P, int nb,
+                          int np, int nx, double D, int mode, int nthreads)
+{
+    oc_fdk_filter_ex(rcov, R, xi, P, NULL, nb, np, nx, D, mode, 0, 0, 0, nthreads);
 }
 
 /* FDK backprojection of filtered projections (FDK.cu:50-126 with the view
@@ -659,63 +780,31 @@ OC_API void oc_fan_bp(float *disp, const float *R, const float *P, const float *
 /* ------------------------------------------------------------------------ */
 /* FBPfan: weight + S-L filter + 1/U^2 weighted BP (FBPfan.cu:21-96).       */
 /* ------------------------------------------------------------------------ */
-OC_API void oc_fbpfan_filter(float *rcov, const float *R, const float *P, int nb, int np,
-                             double rscan, int mode, int nthreads)
+OC_API void oc_fbpfan_filter_ex(float *rcov, const float *R, const float *P, const float *beta, int nb,
+                                int np, double rscan, int mode, int kind, int wlen, int short_scan,
+                                int nthreads)
 {
     set_threads(nthreads);
     float pint = fabsf(P[1] - P[0]);
     float *g = (float *)malloc(sizeof(float) * (2 * np - 1));
-    oc_sl_filter(g, pint, np);
+    oc_ramp_taps(g, kind, pint, np);
     double *w = (double *)malloc(sizeof(double) * np);
     for (int p = 0; p < np; ++p) w[p] = rscan / sqrt(sq(rscan) + sq(P[p]));
-    const int tile = 128, limit = 1024, row_block = 128;   /* FBPfan.h:24-26 */
-#pragma omp parallel
-    {
-        float *cur = (float *)malloc(sizeof(float) * np);
-        int *pos = (int *)malloc(sizeof(int) * (np / tile + 2));
-#pragma omp for schedule(dynamic, 4)
-        for (int row = 0; row < nb; ++row) {
-            const float *in = R + (long)row * np;
-            float *out = rcov + (long)row * np;
-            for (int p = 0; p < np; ++p) out[p] = 0.0f;
-            int gtime = (int)ceil(1.0 * np / limit);
-            if (mode == 0) {
-                for (int p = 0; p < np; ++p) cur[p] = (float)(in[p] * w[p]);
-                for (int c = 0; c < gtime; ++c) {
-                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
-                    for (int p = 0; p < np; ++p) {
-                        double acc = 0;
-                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
-                        out[p] = (float)((double)out[p] + pint * acc);
-                    }
-                }
-                continue;
-            }
-            int nfull = np / tile, resid = np % tile, ntiles = nfull + (resid ? 1 : 0);
-            int in_resid_rows = (nb % row_block) != 0 && row >= (nb / row_block) * row_block;
-            for (int k = 0; k < ntiles; ++k)
-                pos[k] = (in_resid_rows && resid) ? ((k == nfull) ? 0 : k + 1) : k;
-            for (int p = 0; p < np; ++p) cur[p] = in[p];
-            for (int step = 0; step < ntiles; ++step) {
-                int k = 0;
-                for (int j = 0; j < ntiles; ++j) if (pos[j] == step) k = j;
-                int p0 = k * tile, p1 = (k == nfull) ? np : p0 + tile;
-                for (int c = 0; c < gtime; ++c) {
-                    for (int p = p0; p < p1; ++p) cur[p] = (float)(cur[p] * w[p]);
-                    int g0 = c * limit, g1 = (c == gtime - 1) ? np : (c + 1) * limit;
-                    for (int p = p0; p < p1; ++p) {
-                        double acc = 0;
-                        for (int q = g0; q < g1; ++q) acc += cur[q] * g[(np - 1) + p - q];
-                        out[p] = (float)((double)out[p] + pint * acc);
-                    }
-                }
-            }
-        }
-        free(cur);
-        free(pos);
-    }
+    filt_opts o;
+    float *pwb;
+    double *winb;
+    make_opts(&o, &pwb, &winb, beta, nb, P, np, rscan, 1, wlen, short_scan);
+    filter_rows(rcov, R, nb, np, pint, g, w, 1, 128, 1024, 128, nb, mode, &o);   /* FBPfan.h:24-26 */
+    free(pwb);
+    free(winb);
     free(w);
     free(g);
+}
+
+OC_API void oc_fbpfan_filter(float *rcov, const float *R, const float *P, int nb, int np,
+                             double rscan, int mode, int nthreads)
+{
+    oc_fbpfan_filter_ex(rcov, R, P, NULL, nb, np, rscan, mode, 0, 0, 0, nthreads);
 }
 
 OC_API void oc_fbpfan_bp(float *disp, const float *rcov, const float *P, const float *beta, int nb,

@@ -56,6 +56,11 @@ class Oracle:
         lib.oc_par_fp.argtypes = [_f32p, _f64p, _f64p, _f64p, _i, _i, _d, _d, _i, _i, _f64p, _i]
         lib.oc_fan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i]
         lib.oc_fbpfan_filter.argtypes = [_f32p, _f32p, _f32p, _i, _i, _d, _i, _i]
+        lib.oc_ramp_taps.argtypes = [_f32p, _i, C.c_float, _i]
+        lib.oc_hamming.argtypes = [_f64p, _i]
+        lib.oc_parker_weights.argtypes = [_f32p, _f32p, _i, _f32p, _i, _d]
+        lib.oc_fdk_filter_ex.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _i, _i, _i, _d, _i, _i, _i, _i, _i]
+        lib.oc_fbpfan_filter_ex.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _d, _i, _i, _i, _i, _i]
         lib.oc_fbpfan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i]
         lib.oc_fbpfan.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d, _i, _i]
         lib.oc_fbppar.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _i]
@@ -92,6 +97,24 @@ class Oracle:
         self.lib.oc_sl_filter(g, pint, np_)
         return g
 
+    def ramp_taps(self, kind, pint, np_):
+        """Ramp taps: kind 0 Shepp-Logan, 1 Ram-Lak (half amplitude)."""
+        g = np.zeros(2 * np_ - 1, np.float32)
+        self.lib.oc_ramp_taps(g, int(kind), pint, np_)
+        return g
+
+    def hamming(self, m):
+        h = np.zeros(m, np.float64)
+        self.lib.oc_hamming(h, int(m))
+        return h
+
+    def parker_weights(self, beta, P, D):
+        """2 x ParkFunction weights [view][bin] (float32)."""
+        beta, P = _f32(beta), _f32(P)
+        out = np.zeros((len(beta), len(P)), np.float32)
+        self.lib.oc_parker_weights(out.ravel(), beta, len(beta), P, len(P), float(D))
+        return out
+
     def fdk_weight_apply(self, R, P, xi, D):
         R = _f32(R)
         out = np.zeros_like(R)
@@ -111,6 +134,16 @@ class Oracle:
         nb = R.shape[0]
         self.lib.oc_fdk_filter(out.ravel(), R.ravel(), _f32(xi), _f32(P), nb, len(P), len(xi), float(D),
                                int(mode), self.nthreads)
+        return out
+
+    def fdk_filter_ex(self, R, beta, P, xi, D, mode=0, kind=0, window=0, short_scan=False):
+        """FDK filter stage with the filter options (taps kind, smoothing
+        window length, short-scan weights)."""
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fdk_filter_ex(out.ravel(), R.ravel(), _f32(xi), _f32(P), _f32(beta), R.shape[0], len(P),
+                                  len(xi), float(D), int(mode), int(kind), int(window), int(bool(short_scan)),
+                                  self.nthreads)
         return out
 
     def fdk_bp(self, rcov, beta, P, xi, size, D, shape, sticky=1):
@@ -166,6 +199,14 @@ class Oracle:
         out = np.zeros_like(R)
         self.lib.oc_fbpfan_filter(out.ravel(), R.ravel(), _f32(P), R.shape[0], len(P), float(rscan),
                                   int(mode), self.nthreads)
+        return out
+
+    def fbpfan_filter_ex(self, R, beta, P, rscan, mode=0, kind=0, window=0, short_scan=False):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fbpfan_filter_ex(out.ravel(), R.ravel(), _f32(P), _f32(beta), R.shape[0], len(P),
+                                     float(rscan), int(mode), int(kind), int(window), int(bool(short_scan)),
+                                     self.nthreads)
         return out
 
     def fbpfan_bp(self, rcov, beta, P, size, shape, rscan):
@@ -312,6 +353,14 @@ class RefCPU:
         Rw = _f32(Rw).copy()
         out = np.zeros_like(Rw)
         self.libs["fbpfan"].ref_fbpfan_conv(out.ravel(), Rw.ravel(), _f32(P), Rw.shape[0], len(P))
+        return out
+
+    def fbpfan_filter_ex(self, R, beta, P, rscan, mode=0, kind=0, window=0, short_scan=False):
+        R = _f32(R)
+        out = np.zeros_like(R)
+        self.lib.oc_fbpfan_filter_ex(out.ravel(), R.ravel(), _f32(P), _f32(beta), R.shape[0], len(P),
+                                     float(rscan), int(mode), int(kind), int(window), int(bool(short_scan)),
+                                     self.nthreads)
         return out
 
     def fbpfan_bp(self, rcov, beta, P, size, shape, rscan):
