@@ -467,6 +467,48 @@ def run_fan2d(args):
     print(json.dumps(line), flush=True)
 
 
+def run_iterfdk(args):
+    """IterativeFDK error slice of IterativeFDK.m's set-up: 128^3 over 60 mm,
+    PInt 0.4 (234 bins), D 200, 360 views, 221 depth samples, slice t = 64
+    (MATLAB index).  Time per slice, and two views checked against the oracle."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+    import ctgb
+    from ctgb import phantom
+    from ctgb.device import iterfdk_err
+    from ctgb.geometry import iterative_fdk_setup
+    ctgb.load()
+    shape, size, D, t = (128, 128, 128), (60.0, 60.0, 60.0), 200.0, 63
+    beta, U, P, G = iterative_fdk_setup(size, shape, pint=0.4, D=D, n_views=360)
+    pic = phantom.ellipsoids_3d(128, 128, 128, phantom.ellipsoid_params(12, seed=6)).numpy()
+    pic = gaussian_filter(pic, 0.5).astype(np.float32)          # the script's imgaussfilt3(pic, 0.5) prior
+    d_pic = torch.from_numpy(pic).cuda()
+    out = torch.empty((len(beta), 128, 128), dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        iterfdk_err(d_pic, beta, U, P, G, size, D, t, out)
+    ts = []
+    for _ in range(args.steps):
+        e0, e1 = _events()
+        e0.record()
+        iterfdk_err(d_pic, beta, U, P, G, size, D, t, out)
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    tsec = float(np.median(ts))
+    iters = len(beta) * 128 * 128 * len(U) * len(P)
+    line = {"metric": "IterativeFDK error slice ms", "value": tsec * 1e3, "unit": "ms",
+            "inner_iterations": iters, "giter_per_s": iters / tsec / 1e9,
+            "config": {"workload": "IterativeFDK.m set-up: 128^3 / 60 mm, 360 views, LP 234, LU 221, t = 64"}}
+    if not args.no_cpu:
+        from oracle.oracle import Oracle
+        sel = [0, 1, 137]          # the first two keep the scan interval |beta1 - beta0| of the full scan
+        ref = Oracle().iterfdk_err(pic, beta[sel], U, P, G, size, D, t)
+        got = out[sel].cpu().numpy()
+        line["oracle_check"] = {"views": sel, "rel_l2": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                                "bit_identical_fraction": float(np.mean(got == ref))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -477,7 +519,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
     ap.add_argument("--size", choices=["full", "small"], default="full",
                     help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
-    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d"], default="pair",
+    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     args = ap.parse_args()
@@ -488,7 +530,8 @@ def main():
     elif args.workload == "pair":
         run_ours(args)
     else:
-        {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d}[args.workload](args)
+        {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d,
+         "iterfdk": run_iterfdk}[args.workload](args)
 
 
 if __name__ == "__main__":

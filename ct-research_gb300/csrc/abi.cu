@@ -12,6 +12,7 @@
 #include <string>
 #include <vector>
 
+#include "devbuf.cuh"
 #include "kernels.cuh"
 
 namespace ct {
@@ -37,35 +38,6 @@ int sm_count() {
         if (n <= 0) n = 1;
     }
     return n;
-}
-
-// Device buffer that grows on demand.
-struct DevBuf {
-    void *ptr = nullptr;
-    size_t bytes = 0;
-    int ensure(size_t n) {
-        if (n <= bytes) return CT_OK;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-        CT_CUDA(cudaMalloc(&ptr, n), "cudaMalloc");
-        bytes = n;
-        return CT_OK;
-    }
-    void release() {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-    }
-    template <typename T> T *as() const { return reinterpret_cast<T *>(ptr); }
-};
-
-template <typename T>
-static int upload(DevBuf &b, const T *host, size_t n) {
-    int s = b.ensure(sizeof(T) * n);
-    if (s) return s;
-    CT_CUDA(cudaMemcpy(b.ptr, host, sizeof(T) * n, cudaMemcpyHostToDevice), "upload");
-    return CT_OK;
 }
 
 // List of grazing rays for the FP64 re-walk (ref_walk.cu); allocated on first use.

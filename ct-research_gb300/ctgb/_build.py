@@ -22,7 +22,7 @@ LIB = LIBDIR / "libctgb.so"
 OBJDIR = LIBDIR / "obj"
 
 SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu", "ref_walk.cu", "fan_batch.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "iterfdk.cu"]
 # ref_walk.cu replays the reference's FP64 walk operation by operation: no FMA contraction
 PER_FILE_FLAGS = {"ref_walk.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -36,7 +36,9 @@ def nvcc() -> str:
 
 
 def _flags(extra: list[str] | None = None) -> list[str]:
-    return ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-O2", f"-I{INCLUDE}", f"-I{CSRC}",
+    # host code: no FMA contraction, so host-built tables round as the oracle's on every CPU
+    return ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", f"-I{INCLUDE}",
+            f"-I{CSRC}",
             "--expt-relaxed-constexpr", *(extra or [])]
 
 

@@ -200,6 +200,22 @@ class FanPlan:
         return out
 
 
+def iterfdk_err(pic: torch.Tensor, beta, U, P, G, size, D: float, t: int, out: torch.Tensor | None = None):
+    """IterativeFDK error slice of image slice t (0-based) of the CUDA volume
+    pic [z][s][t]: returns [beta][z][s] float32 on the device (ct_iterfdk_err)."""
+    nz, ns, nt = pic.shape
+    beta = np.ascontiguousarray(beta, np.float32)
+    U = np.ascontiguousarray(U, np.float32)
+    P = np.ascontiguousarray(P, np.float64)
+    G = np.ascontiguousarray(G, np.float64)
+    size = np.ascontiguousarray(size, np.float64)
+    if out is None:
+        out = torch.empty((len(beta), nz, ns), dtype=torch.float32, device=pic.device)
+    _lib.call("ct_iterfdk_err", _tptr(pic), _tptr(out), _np_ptr(beta), len(beta), _np_ptr(U), len(U), _np_ptr(P),
+              len(P), _np_ptr(G), len(G), _np_ptr(size), nt, ns, nz, float(D), int(t), _stream())
+    return out
+
+
 def tv_flow(x: torch.Tensor, iters: int, step: float, eps: float = 1e-8, lo: float = 0.0, work=None, scratch=None):
     """Normalised isotropic TV gradient-flow sub-iterations on x ([nz][ny][nx] or [ny][nx]), in place."""
     if x.dim() == 2:

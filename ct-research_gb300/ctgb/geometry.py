@@ -147,3 +147,33 @@ def config_batched_fan(n_slices: int = 64, seed: int = 4):
         nd = int(rng.integers(256, 1025))
         out.append(fan_config(n, nv, nd, 500.0, float(n), name=f"slice{i}"))
     return out
+
+
+def iterative_fdk_setup(size, shape, pint: float = 0.4, D: float = 200.0, n_views: int = 360):
+    """Domains of the IterativeFDK error computation, as IterativeFDK.m sets
+    them up (:20-60 and :294-312): returns (beta float32, U float32, P float64,
+    G float64).
+
+    * P: -MaxP .. MaxP in steps of pint, MaxP = 1.1 * max(Size) * sqrt(2)/2;
+    * beta: n_views angles k * 2pi/n_views, k = 1..n_views;
+    * U: LU = floor(2 Rpic / dU) depths Rpic - dU * (1..LU) along the ray,
+      Rpic = max(Size) * sqrt(3)/2 and dU = max(Size) / t_length;
+    * G: the Shepp-Logan taps of pint in double, 2 LP - 1 of them.
+    """
+    size = [float(x) for x in size]
+    nz, ns, nt = shape
+    ms = max(size)
+    maxp = 1.1 * ms * np.sqrt(2.0) / 2.0
+    n_p = int(np.floor(2 * maxp / pint + 1e-9)) + 1
+    P = -maxp + pint * np.arange(n_p, dtype=np.float64)
+    beta = (np.arange(1, n_views + 1) * (2 * np.pi / n_views)).astype(np.float32)
+    rpic = ms * np.sqrt(3.0) / 2.0
+    du = ms / nt
+    lu = int(np.floor(2 * rpic / du))
+    U = (rpic - du * np.arange(1, lu + 1)).astype(np.float32)
+    n = np.arange(1, n_p, dtype=np.float64)
+    G = np.zeros(2 * n_p - 1)
+    G[n_p - 1] = 1.0 / (np.pi * pint) ** 2
+    G[n_p - 1 + n.astype(int)] = G[n_p - 1 - n.astype(int)] = -1.0 / (np.pi * pint) ** 2 / (4 * n ** 2 - 1)
+    return beta, U, P, G
+

@@ -15,6 +15,8 @@ sinogram size), in the reference layouts:
   BackprojectionFan2D(R, BetaScanRange, Pdomain, Size, t, s, Rscan)          BackprojectionFan2D.cpp:7-39
   FBPfan(R, BetaScanRange, Pdomain, Size, t, s, Rscan)                       FBPfan.cpp:7-40
   FBPparallel(R, ThetaScanRange, Tdomain, Size, t, s)                        FBPparallel.cpp:7-38
+  IterativeFDKerrCompute(Pic, t, s, z, Size, BetaScanRange, Udomain, Pdomain, Distance, G, t_slice)
+      IterativeFDKerrCompute.cpp:3-58 -> error slice [beta][z][s]
 
 Domain vectors are read with their length as MATLAB's mxGetM would (any
 1-D array-like).  Single-precision arguments are converted to float32 and
@@ -167,3 +169,28 @@ def Vec2img_Cpp2Mat2D(vec, height, width):
     """fliplr(reshape(vec, height, width))' -- inverse of Img2vec_Mat2Cpp2D."""
     m = np.asarray(vec).reshape((height, width), order="F")
     return np.fliplr(m).T
+
+
+def IterativeFDKerrCompute(Pic, t_length, s_length, z_length, Size, BetaScanRange, Udomain, Pdomain, Distance, G,
+                           t, on_error="raise"):
+    """Error slice of the iterative FDK for image slice t (MATLAB index, from 1):
+    LBeta * s_length * z_length values laid out [beta][z][s], the derivation of
+    the gateway's scalars included (IterativeFDKerrCompute.cpp:5-31).
+    BetaScanRange and Udomain are single, Pdomain and G double."""
+    pic = _f32(Pic)
+    nt, ns, nz = int(t_length), int(s_length), int(z_length)
+    if pic.size != nt * ns * nz:
+        raise ValueError("Pic must hold t_length*s_length*z_length values")
+    Size = _f64(Size)
+    beta, U = _f32(BetaScanRange), _f32(Udomain)
+    P, G = _f64(Pdomain), _f64(G)
+    res = _f64([Size[0] / nt, Size[1] / ns, Size[2] / nz])
+    out = np.zeros(len(beta) * ns * nz, np.float32)
+    bint = np.float32(abs(beta[1] - beta[0])) if len(beta) > 1 else np.float32(0)
+    du = np.float32(abs(U[1] - U[0])) if len(U) > 1 else np.float32(0)
+    pint = abs(P[1] - P[0]) if len(P) > 1 else 0.0
+    _run("ct_IterativeFDKerrCompute", out, on_error, _ptr(pic), _ptr(out), _ptr(beta), _ptr(U), _ptr(P), _ptr(G),
+         _ptr(Size), nt, ns, nz, Size[0] / 2, Size[1] / 2, Size[2] / 2, len(beta), len(P), len(U), len(G),
+         float(Distance), _ptr(res), int(t) - 1, float(bint), float(du), float(pint))
+    return out.astype(np.float64)
+

@@ -231,6 +231,30 @@ int ct_fan_batch_fbp(ct_fan_batch *batch, const float *d_proj, float *d_img, int
 int ct_fan_batch_set_filter(ct_fan_batch *batch, int kind, int window_len, int short_scan);
 
 /* ===================================================================== */
+/* IterativeFDK error slice                                               */
+/* ===================================================================== */
+
+/* Drop-in for IterativeFDKerrCompute() (IterativeFDKerrCompute.h:23-27): host
+ * pointers, the reference's argument list and meaning.  Pic is the prior image
+ * [z][s][t]; ErrorSlicecuda receives LBeta * s_length * z_length floats laid
+ * out [beta][z][s] for image slice t (0-based).  Every (s, z) is computed once
+ * at any size (the reference's residual launches cover s, z < 512 or
+ * multiples of 512 only). */
+int ct_IterativeFDKerrCompute(const float *Pic, float *ErrorSlicecuda, const float *BetaScanRange,
+                              const float *Udomain, const double *Pdomain, const double *G,
+                              const double *Size, int t_length, int s_length, int z_length,
+                              double Center_t, double Center_s, double Center_z, int LBeta, int LP,
+                              int LU, int LG, double Distance, const double *resolution2, int t,
+                              float BetaScanInt, float dU, double PInt);
+/* Device-pointer form: d_Pic and d_Err on the device, the domains on the host;
+ * centres, resolution and intervals derived as the MEX gateway does
+ * (IterativeFDKerrCompute.cpp:10-31).  t is 0-based. */
+int ct_iterfdk_err(const float *d_Pic, float *d_Err, const float *BetaScanRange, int LBeta,
+                   const float *Udomain, int LU, const double *Pdomain, int LP, const double *G, int LG,
+                   const double *Size, int t_length, int s_length, int z_length, double Distance, int t,
+                   void *stream);
+
+/* ===================================================================== */
 /* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */
 /* ===================================================================== */
 

@@ -48,6 +48,8 @@ REF_UNITS = [
     ("fbppar", "Analytic_Algorithm/FBP_type_analytic_algorithm_GPU_cpp_sourcecode/FBP_parallel_GPU/FBPparallel.cu",
      "Analytic_Algorithm/FBP_type_analytic_algorithm_GPU_cpp_sourcecode/FBP_parallel_GPU/FBPparallel.h",
      ["GFunction", "Filter", "BackProjection"], "harness_fbppar.cpp"),
+    ("iterfdk", "My_novel_algorithm/IterativeFDK/IterativeFDKerrCompute.cu",
+     "My_novel_algorithm/IterativeFDK/IterativeFDKerrCompute.h", ["IterativeFDKerr"], "harness_iterfdk.cpp"),
 ]
 
 

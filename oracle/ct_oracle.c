@@ -903,6 +903,67 @@ OC_API void oc_fbppar(float *disp, const float *R, const float *T, const float *
 }
 
 /* ------------------------------------------------------------------------ */
+/* IterativeFDK error slice (IterativeFDKerrCompute.cu:12-76): for the image  */
+/* slice t, every (view, z, s) gathers, over the U samples along each ray of  */
+/* the view and every detector bin P, the weighted difference between the     */
+/* prior image at the ray point's depth and at the voxel's own z.  Output     */
+/* [beta][z][s]; the sum is a float accumulator updated in double, U major    */
+/* and P minor, as the reference's per-(view, U) launches add into it.        */
+/* Arguments are those of the MEX gateway (IterativeFDKerrCompute.cpp:5-31): */
+/* BetaScanInt = |b1 - b0| and dU = |U1 - U0| in float, PInt = |P1 - P0|.     */
+/* ------------------------------------------------------------------------ */
+OC_API void oc_iterfdk_err(const float *pic, float *err, const float *beta, const float *U,
+                           const double *P, const double *G, const double *size, int nt, int ns, int nz,
+                           int nb, int np, int nu, int lg, double D, int t, int nthreads)
+{
+    set_threads(nthreads);
+    const double res[3] = {size[0] / nt, size[1] / ns, size[2] / nz};
+    const double ct = size[0] / 2, cs = size[1] / 2, cz = size[2] / 2;
+    const float bint = fabsf(beta[1] - beta[0]);
+    const float du = fabsf(U[1] - U[0]);
+    const double pint = fabs(P[1] - P[0]);
+    const long plane = (long)nt * ns;
+#pragma omp parallel for collapse(2) schedule(dynamic, 8)
+    for (int b = 0; b < nb; ++b)
+        for (int z = 0; z < nz; ++z) {
+            const float sb = sinf(beta[b]), cb = cosf(beta[b]);
+            for (int s = 0; s < ns; ++s) {
+                const float it = (float)((t + 0.5) * res[0] - ct);
+                const float is = (float)((s + 0.5) * res[1] - cs);
+                const float iz = (float)((z + 0.5) * res[2] - cz);
+                const float dt = it * cb + is * sb;      /* rotated frame */
+                const float ds = -it * sb + is * cb;
+                const float dz = iz;
+                const float lr = (float)(D / (D - ds));
+                const float a = dt * lr;
+                float acc = 0.0f;
+                for (int u = 0; u < nu; ++u) {
+                    const float uu = U[u];
+                    const float zr = (float)(dz + (ds - uu) * dz / (D - ds));
+                    const int zi = (int)floor((zr + cz) / res[2]);
+                    for (int p = 0; p < np; ++p) {
+                        const double pv = P[p];
+                        const int fi = (int)(floor((a - pv) / pint) + np);
+                        if (fi < 0 || fi >= lg) continue;
+                        const float tr = (float)(pv * (D - uu) / D);
+                        const float xr = tr * cb - uu * sb;
+                        const float yr = tr * sb + uu * cb;
+                        const int xi = (int)floor((xr + ct) / res[0]);
+                        const int yi = (int)floor((yr + cs) / res[1]);
+                        if (xi < 0 || xi >= nt || yi < 0 || yi >= ns || zi < 0 || zi >= nz) continue;
+                        const long col = (long)yi * nt + xi;
+                        const float diff = pic[zi * plane + col] - pic[z * plane + col];
+                        const double term = 0.5 * (1.0 * lr * lr) * diff * sqrt(1 + 1.0 * (pv / D) * (pv / D))
+                                            * G[fi] * D / sqrt(1.0 * D * D + 1.0 * pv * pv) * du * pint * bint;
+                        acc = (float)(acc + term);
+                    }
+                }
+                err[((long)b * nz + z) * ns + s] = acc;
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Independent check: textbook alpha-Siddon line integral through a t,s,z   */
 /* grid (the merge-of-plane-crossings form of Siddon3D.m /                  */
 /* GenSysMatCircular3D.m), FP64.  Used by the tests as a second oracle that */

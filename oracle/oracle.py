@@ -69,6 +69,8 @@ class Oracle:
         lib.oc_cone_segments.argtypes = [_i, _i, _i, _f64p, _d, _d, _d, _f32p, _f32p, _f32p,
                                          _i, _i, _i, _d, _i, _i]
         lib.oc_cone_segments.restype = C.c_longlong
+        lib.oc_iterfdk_err.argtypes = [_f32p, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p, _i, _i, _i, _i, _i, _i,
+                                       _i, _d, _i, _i]
 
     # -- 3D cone ------------------------------------------------------------
     def cone_fp(self, vol, beta, P, xi, size, D):
@@ -230,6 +232,16 @@ class Oracle:
                            _f64(size), nt, ns, self.nthreads)
         return out
 
+    def iterfdk_err(self, pic, beta, U, P, G, size, D, t):
+        """IterativeFDKerrCompute: error slice [beta][z][s] of image slice t
+        (0-based here; the MEX gateway subtracts 1 from its MATLAB index)."""
+        pic = _f32(pic)
+        nz, ns, nt = pic.shape
+        out = np.zeros((len(beta), nz, ns), np.float32)
+        self.lib.oc_iterfdk_err(pic.ravel(), out.ravel(), _f32(beta), _f32(U), _f64(P), _f64(G), _f64(size), nt, ns,
+                                nz, len(beta), len(P), len(U), len(G), float(D), int(t), self.nthreads)
+        return out
+
     # -- independent checks ---------------------------------------------------
     def siddon_line(self, vol, size, src, dst):
         vol = _f32(vol)
@@ -275,6 +287,8 @@ class RefCPU:
         L["fbpfan"].ref_fbpfan_conv.argtypes = [_f32p, _f32p, _f32p, _i, _i]
         L["fbpfan"].ref_fbpfan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d]
         L["fbppar"].ref_fbppar.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i]
+        L["iterfdk"].ref_iterfdk_err.argtypes = [_f32p, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p, _i, _i, _i, _i,
+                                                 _i, _i, _i, _d, _i]
 
     def cone_fp(self, vol, beta, P, xi, size, D):
         vol = _f32(vol)
@@ -375,6 +389,18 @@ class RefCPU:
         out = np.zeros(shape, np.float32)
         self.libs["fbppar"].ref_fbppar(out.ravel(), _f32(R).ravel(), _f32(T), _f32(theta), len(theta), len(T),
                                        _f64(size), nt, ns)
+        return out
+
+    def iterfdk_err(self, pic, beta, U, P, G, size, D, t):
+        """IterativeFDKerrCompute: error slice [beta][z][s] of image slice t (1-based)."""
+        pic = _f32(pic)
+        nz, ns, nt = pic.shape
+        out = np.zeros((len(beta), nz, ns), np.float32)
+        st = self.libs["iterfdk"].ref_iterfdk_err(pic.ravel(), out.ravel(), _f32(beta), _f32(U), _f64(P), _f64(G),
+                                                  _f64(size), nt, ns, nz, len(beta), len(P), len(U), len(G),
+                                                  float(D), int(t))
+        if st:
+            raise ValueError("reference harness drives s_length, z_length < 512 only")
         return out
 
 

@@ -101,7 +101,24 @@ def main():
                         fbp_weighted=fw, fbp_conv=fconv, fbp_bp=fbp, fbppar=fbppar).items():
         out[f"f2_{name}"] = v
 
+    # --- IterativeFDK error slice (IterativeFDKerrCompute.cu) -----------------
+    from scipy.ndimage import gaussian_filter
+    from ctgb.geometry import iterative_fdk_setup
+    ishape, isize = (16, 18, 20), [20.0, 18.0, 16.0]
+    ibeta, iU, iP, iG = iterative_fdk_setup(isize, ishape, pint=0.8, D=70.0, n_views=10)
+    ipic = phantom.ellipsoids_3d(20, 18, 16, phantom.ellipsoid_params(8, seed=11)).numpy()
+    ipic = f32(gaussian_filter(ipic, 0.7))
+    for name, v in dict(pic=ipic, beta=ibeta, U=iU, P=iP, G=iG, size=np.asarray(isize), D=np.asarray(70.0)).items():
+        out[f"ifdk_{name}"] = v
+    for t in (1, 10):
+        out[f"ifdk_err_t{t}"] = ref.iterfdk_err(ipic, ibeta, iU, iP, iG, isize, 70.0, t)
+
     dst = Path(__file__).resolve().parent / "reference_kernels.npz"
+    if dst.exists():
+        old = np.load(dst)
+        changed = [k for k in old.files if k in out and not np.array_equal(old[k], out[k])]
+        if changed:
+            print("warning: fixtures changed:", changed)
     np.savez_compressed(dst, **out)
     print(dst, sum(v.nbytes for v in out.values()), "bytes raw,", dst.stat().st_size, "on disk")
 

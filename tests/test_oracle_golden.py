@@ -92,3 +92,13 @@ def test_fbpparallel_matches_reference(oracle, golden):
     out = oracle.fbppar(golden["f2_par"].astype(np.float32), golden["f2_beta"].astype(np.float32),
                         golden["f2_P"].astype(np.float32), golden["f2_size"], (30, 32))
     assert rel_l2(out, golden["f2_fbppar"]) <= TOL
+
+
+@pytest.mark.parametrize("t", [1, 10])
+def test_iterative_fdk_error_matches_reference(oracle, golden, t):
+    g = {n: golden[f"ifdk_{n}"] for n in ("pic", "beta", "U", "P", "G", "size", "D")}
+    ref = golden[f"ifdk_err_t{t}"]
+    out = oracle.iterfdk_err(g["pic"], g["beta"], g["U"], g["P"], g["G"], g["size"], float(g["D"]), t - 1)
+    assert np.count_nonzero(ref) > ref.size // 2        # the case exercises the gathers
+    assert rel_l2(out, ref) <= TOL
+    assert np.mean(out == ref) > 0.99
