@@ -509,6 +509,43 @@ def run_iterfdk(args):
     print(json.dumps(line), flush=True)
 
 
+def run_fdkui(args):
+    """Curved-detector short-scan FDK of the scanner set-up of ImplementUIData.m:
+    936 gammas x 80 rows x 800 views (240 deg) into 512 x 512 x 50 (23 mm),
+    D 570, SDD 1060.2; smooth synthetic double projections."""
+    import torch
+    import ctgb
+    from ctgb.device import fdkui_bp, fdkui_filter
+    from ctgb.geometry import curved_fdk_case
+    ctgb.load()
+    c = curved_fdk_case("scanner")
+    b = torch.tensor(c["beta"], device="cuda").view(-1, 1, 1)
+    x = torch.tensor(c["xi"], device="cuda").view(1, -1, 1)
+    g = torch.tensor(c["gama"], device="cuda").view(1, 1, -1)
+    R = ((1.0 + 0.3 * torch.cos(b + 0.01 * x)) * (1 - (g / g.abs().max()) ** 2).clamp_(min=0)).contiguous()
+    rcov = torch.empty(R.shape, dtype=torch.float32, device="cuda")
+    disp = torch.empty((c["z_length"], 512, 512), dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        fdkui_filter(R, c["xi"], c["gama"], c["beta"], c["b0"], c["maxg"], c["D"], c["ds2d"], rcov)
+        fdkui_bp(rcov, c["xi"], c["gama"], c["beta"], c["D"], c["ds2d"], c["size"], c["z_length"], disp)
+    ts = []
+    for _ in range(args.steps):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        fdkui_filter(R, c["xi"], c["gama"], c["beta"], c["b0"], c["maxg"], c["D"], c["ds2d"], rcov)
+        e[1].record()
+        fdkui_bp(rcov, c["xi"], c["gama"], c["beta"], c["D"], c["ds2d"], c["size"], c["z_length"], disp)
+        e[2].record()
+        torch.cuda.synchronize()
+        ts.append((e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])))
+    tf, tb = float(np.median([a for a, _ in ts])), float(np.median([q for _, q in ts]))
+    line = {"metric": "curved-detector FDK ms", "value": tf + tb, "unit": "ms", "filter_ms": tf, "bp_ms": tb,
+            "filter_macs": 800 * 80 * 936 * 936, "bp_voxel_views": 512 * 512 * 50 * 800,
+            "config": {"workload": "ImplementUIData.m set-up: 936 x 80 x 800 (240 deg) -> 512 x 512 x 50, "
+                                   "D 570, SDD 1060.2"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -519,7 +556,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
     ap.add_argument("--size", choices=["full", "small"], default="full",
                     help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
-    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk"], default="pair",
+    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     args = ap.parse_args()
@@ -531,7 +568,7 @@ def main():
         run_ours(args)
     else:
         {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d,
-         "iterfdk": run_iterfdk}[args.workload](args)
+         "iterfdk": run_iterfdk, "fdkui": run_fdkui}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -216,6 +216,32 @@ def iterfdk_err(pic: torch.Tensor, beta, U, P, G, size, D: float, t: int, out: t
     return out
 
 
+def fdkui_filter(R: torch.Tensor, xi, gama, beta, b0: float, fan: float, D: float, ds2d: float, out=None):
+    """Curved-detector FDK filter stage on the device: R float64 [beta][xi][gamma]
+    -> weighted, filtered rows as float32 (ct_fdkui_filter)."""
+    if R.dtype != torch.float64 or not R.is_cuda or not R.is_contiguous():
+        raise ValueError("R must be a contiguous float64 CUDA tensor")
+    nb, lx, lg = R.shape
+    xi, gama, beta = (np.ascontiguousarray(a, np.float64) for a in (xi, gama, beta))
+    out = torch.empty(R.shape, dtype=torch.float32, device=R.device) if out is None else out
+    _lib.call("ct_fdkui_filter", C.c_void_p(R.data_ptr()), _tptr(out), _np_ptr(xi), _np_ptr(gama), _np_ptr(beta),
+              float(b0), float(fan), float(D), float(ds2d), lg, nb, lx, _stream())
+    return out
+
+
+def fdkui_bp(rcov: torch.Tensor, xi, gama, beta, D: float, ds2d: float, size, z_length: int, out=None):
+    """Curved-detector FDK backprojection of float32 rcov [beta][xi][gamma] into a
+    float64 display [z][s][t] (ct_fdkui_bp)."""
+    nb, lx, lg = rcov.shape
+    xi, gama, beta = (np.ascontiguousarray(a, np.float64) for a in (xi, gama, beta))
+    size = np.ascontiguousarray(size, np.int32)
+    if out is None:
+        out = torch.empty((int(z_length), int(size[1]), int(size[0])), dtype=torch.float64, device=rcov.device)
+    _lib.call("ct_fdkui_bp", _tptr(rcov), C.c_void_p(out.data_ptr()), _np_ptr(xi), _np_ptr(gama), _np_ptr(beta),
+              float(D), float(ds2d), lg, nb, lx, _np_ptr(size), int(z_length), _stream())
+    return out
+
+
 def tv_flow(x: torch.Tensor, iters: int, step: float, eps: float = 1e-8, lo: float = 0.0, work=None, scratch=None):
     """Normalised isotropic TV gradient-flow sub-iterations on x ([nz][ny][nx] or [ny][nx]), in place."""
     if x.dim() == 2:

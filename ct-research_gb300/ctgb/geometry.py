@@ -177,3 +177,40 @@ def iterative_fdk_setup(size, shape, pint: float = 0.4, D: float = 200.0, n_view
     G[n_p - 1 + n.astype(int)] = G[n_p - 1 - n.astype(int)] = -1.0 / (np.pi * pint) ** 2 / (4 * n ** 2 - 1)
     return beta, U, P, G
 
+
+def curved_fdk_case(kind: str = "filter"):
+    """Inputs of the curved-detector FDK cases (the scanner set-up of
+    ImplementUIData.m:7-36 and small variants).  Returns a dict with gama
+    (descending, as the script negates the detector angles), xi, beta, b0,
+    maxg (the fan angle |gama_end - gama_1|), D, ds2d and, for "bp", the
+    display Size and z_length.
+
+    * "filter": the reference's fixed detector (936 gammas at 9.7527e-4 rad,
+      80 rows at 0.915 mm), D 570, SDD 1060.2, five views chosen across the
+      three Parker regions.
+    * "bp": a small detector (120 x 16) and a 40 x 36 x 10 display, D 100.
+    * "scanner": the script's full set-up, 800 views over 240 deg from 1.5466 deg
+      and a 512 x 512 x 50 display over 23 mm.
+    """
+    if kind in ("filter", "scanner"):
+        gint = 9.7527e-4
+        gama = -(np.arange(936) - 467.5) * gint
+        xi = (np.arange(80) - 39.5) * 0.915
+        b0 = np.deg2rad(1.5466)
+        d = dict(gama=gama, xi=xi, b0=b0, maxg=abs(gama[-1] - gama[0]), D=570.0, ds2d=1060.2)
+        if kind == "filter":
+            d["beta"] = b0 + np.array([0.0, 0.3, 1.4, np.pi - 0.2, np.pi + 0.55])
+        else:
+            bint = np.deg2rad(240 / 800)
+            d["beta"] = b0 + bint * np.arange(800)
+            d["size"], d["z_length"] = np.array([512, 512, 23], np.int32), 50
+        return d
+    if kind == "bp":
+        gama = -(np.arange(120) - 59.5) * 0.0075
+        xi = (np.arange(16) - 7.5) * 2.2
+        b0 = 0.05
+        beta = b0 + np.arange(90) * (2 * np.pi / 90)
+        return dict(gama=gama, xi=xi, beta=beta, b0=b0, maxg=abs(gama[-1] - gama[0]), D=100.0, ds2d=180.0,
+                    size=np.array([40, 36, 13], np.int32), z_length=10)
+    raise ValueError(kind)
+

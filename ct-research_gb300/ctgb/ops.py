@@ -17,6 +17,8 @@ sinogram size), in the reference layouts:
   FBPparallel(R, ThetaScanRange, Tdomain, Size, t, s)                        FBPparallel.cpp:7-38
   IterativeFDKerrCompute(Pic, t, s, z, Size, BetaScanRange, Udomain, Pdomain, Distance, G, t_slice)
       IterativeFDKerrCompute.cpp:3-58 -> error slice [beta][z][s]
+  ImplementUI(R, Xigamadomain, Gamadomain, BetaScanRange, StartAngle, GamaMax, Distance, Distance_s2d, Size, z_length)
+      ImplementUI.cpp:3-58 -> curved-detector FDK display [z][s][t]
 
 Domain vectors are read with their length as MATLAB's mxGetM would (any
 1-D array-like).  Single-precision arguments are converted to float32 and
@@ -193,4 +195,21 @@ def IterativeFDKerrCompute(Pic, t_length, s_length, z_length, Size, BetaScanRang
          _ptr(Size), nt, ns, nz, Size[0] / 2, Size[1] / 2, Size[2] / 2, len(beta), len(P), len(U), len(G),
          float(Distance), _ptr(res), int(t) - 1, float(bint), float(du), float(pint))
     return out.astype(np.float64)
+
+
+def ImplementUI(R, Xigamadomain, Gamadomain, BetaScanRange, betaStartAngle, MaxGama, Distance, Distance_s2d, Size,
+                z_length, on_error="raise"):
+    """Curved-detector short-scan FDK (ImplementUI.cpp:5-26): R double
+    [beta][xi][gamma] -> float64 column vector of Size[0]*Size[1]*z_length
+    values laid out [z][s][t].  Size is cast to int as the gateway does."""
+    R = _f64(R)
+    xi, gama, beta = _f64(Xigamadomain), _f64(Gamadomain), _f64(BetaScanRange)
+    size = np.ascontiguousarray([int(v) for v in np.asarray(Size, np.float64).ravel()[:3]], np.int32)
+    nz = int(z_length)
+    if R.size != len(xi) * len(gama) * len(beta):
+        raise ValueError("R must hold LGama*LXigama*LBeta values")
+    out = np.zeros(int(size[0]) * int(size[1]) * nz, np.float64)
+    _run("ct_FDKUI", out, on_error, _ptr(out), _ptr(R), _ptr(xi), _ptr(gama), _ptr(beta), float(betaStartAngle),
+         float(MaxGama), float(Distance), float(Distance_s2d), len(gama), len(beta), len(xi), _ptr(size), nz)
+    return out
 

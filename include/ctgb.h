@@ -255,6 +255,28 @@ int ct_iterfdk_err(const float *d_Pic, float *d_Err, const float *BetaScanRange,
                    void *stream);
 
 /* ===================================================================== */
+/* Curved-detector (equiangular) short-scan FDK                           */
+/* ===================================================================== */
+
+/* Drop-in for FDKUI() (ImplementUI.h:31-33): R [beta][xi][gamma] (double,
+ * LBeta x LXigama x LGama, host) -> Display [z][s][t] (double, Size[0] x
+ * Size[1] x z_length, host).  Size holds the integer extents (pixels in t
+ * and s, mm in z); betaStartAngle and MaxGama feed the Parker weights.  The
+ * reference fixes LGama = 936, LXigama = 80, LBeta = 800 in its filter
+ * launch (ImplementUI.h:16-20); any sizes are accepted here. */
+int ct_FDKUI(double *Display, const double *R, const double *Xigamadomain, const double *Gamadomain,
+             const double *BetaScanRange, double betaStartAngle, double MaxGama, double Distance,
+             double Distance_s2d, int LGama, int LBeta, int LXigama, const int *Size, int z_length);
+/* The two stages on device buffers: weighted, filtered rows of d_R into d_Rcov
+ * (float, same layout), and the backprojection of d_Rcov into d_Display. */
+int ct_fdkui_filter(const double *d_R, float *d_Rcov, const double *Xigamadomain, const double *Gamadomain,
+                    const double *BetaScanRange, double betaStartAngle, double MaxGama, double Distance,
+                    double Distance_s2d, int LGama, int LBeta, int LXigama, void *stream);
+int ct_fdkui_bp(const float *d_Rcov, double *d_Display, const double *Xigamadomain, const double *Gamadomain,
+                const double *BetaScanRange, double Distance, double Distance_s2d, int LGama, int LBeta,
+                int LXigama, const int *Size, int z_length, void *stream);
+
+/* ===================================================================== */
 /* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */
 /* ===================================================================== */
 

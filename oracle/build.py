@@ -50,7 +50,13 @@ REF_UNITS = [
      ["GFunction", "Filter", "BackProjection"], "harness_fbppar.cpp"),
     ("iterfdk", "My_novel_algorithm/IterativeFDK/IterativeFDKerrCompute.cu",
      "My_novel_algorithm/IterativeFDK/IterativeFDKerrCompute.h", ["IterativeFDKerr"], "harness_iterfdk.cpp"),
+    ("fdkui", "My_toolbox/Implement_UnitedImaging_Data/ImplementUI.cu",
+     "My_toolbox/Implement_UnitedImaging_Data/ImplementUI.h", ["GFunction", "PreWeightFiltration", "BackProjection"],
+     "harness_fdkui.cpp"),
 ]
+# units whose kernels synchronise a block between dependent phases: compiled
+# with the shim's threaded mode (one OS thread per simulated thread, real barrier)
+THREADED_UNITS = {"fdkui"}
 
 
 def reference_root() -> Path:
@@ -118,13 +124,14 @@ def build_ref(force: bool = False) -> list[Path]:
             continue
         cu_text = _strip_comments((root / cu).read_text(errors="replace"))
         h_text = _strip_comments((root / h).read_text(errors="replace"))
-        parts = [shim, "\n"]
+        parts = ["#define SHIM_THREADED 1\n"] if name in THREADED_UNITS else []
+        parts += [shim, "\n"]
         parts += [m + "\n" for m in _extract_macros(h_text)]
         parts += [m + "\n" for m in _extract_macros(cu_text)]
         parts += [c + "\n" for c in _extract_device_consts(cu_text)]
         parts += [_extract_function(cu_text, k) + "\n" for k in kernels]
         parts.append((HERE / "shim" / harness).read_text())
-        cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-x", "c++", "-",
+        cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-pthread", "-x", "c++", "-",
                "-o", str(out)]
         subprocess.run(cmd, input="".join(parts).encode(), check=True)
     return outs

@@ -903,6 +903,130 @@ OC_API void oc_fbppar(float *disp, const float *R, const float *T, const float *
 }
 
 /* ------------------------------------------------------------------------ */
+/* Curved-detector (equiangular) FDK of ImplementUI.cu: per-xi-row S-L taps   */
+/* of the equiangular detector (GFunction :6-22), Parker short-scan weight     */
+/* with the cone-tilt proportion, cosine weight and convolution               */
+/* (PreWeightFiltration :25-86), and the 1/L2 weighted backprojection         */
+/* (BackProjection :88-150).  All double, as the reference (R is double).      */
+/* Layouts: R and rcov [view][xi][gamma], display [z][s][t]; Size holds the   */
+/* integer extents of the display in pixels (t, s) and mm (z).                */
+/* ------------------------------------------------------------------------ */
+static double ui_prop(double ds2d, double xi) { return ds2d / sqrt(1.0 * ds2d * ds2d + 1.0 * xi * xi); }
+
+OC_API void oc_fdkui_taps(double *G, double gint, const double *xi, int lx, int lg, double ds2d)
+{
+    const long fs = 2L * lg - 1;
+    for (int x = 0; x < lx; ++x) {
+        const double gp = gint * ui_prop(ds2d, xi[x]);
+        double *g = G + x * fs;
+        g[lg - 1] = 2.0 / (1.0 * (OC_PI * gp) * (OC_PI * gp));
+        for (int n = 1; n < lg; ++n) {
+            const double sn = sin(n * gp);
+            const double v = -2.0 * (1.0 * n * n) / (1.0 * OC_PI * OC_PI) / (4 * (1.0 * n * n) - 1) / (1.0 * sn * sn);
+            g[lg - 1 - n] = v;
+            g[lg - 1 + n] = v;
+        }
+    }
+}
+
+OC_API void oc_fdkui_filter(double *rcov, const double *R, const double *xi, const double *gama,
+                            const double *beta, double b0, double maxg, double D, double ds2d, int lg, int nb,
+                            int lx, int nthreads)
+{
+    set_threads(nthreads);
+    const double gint = fabs(gama[1] - gama[0]);
+    const long fs = 2L * lg - 1;
+    double *G = (double *)malloc(sizeof(double) * fs * lx);
+    oc_fdkui_taps(G, gint, xi, lx, lg, ds2d);
+#pragma omp parallel
+    {
+        double *w = (double *)malloc(sizeof(double) * lg);
+#pragma omp for schedule(dynamic, 4)
+        for (long row = 0; row < (long)nb * lx; ++row) {
+            const int b = (int)(row / lx), x = (int)(row % lx);
+            const double pr = ui_prop(ds2d, xi[x]);
+            const double bp = beta[b] * pr, b0p = b0 * pr, mgp = maxg * pr;
+            const double gip = gint * pr, dp = D / pr;
+            const double *in = R + row * lg;
+            for (int g = 0; g < lg; ++g) {
+                const double gp = gama[g] * pr;
+                double W;
+                if (bp >= b0p && bp < b0p + mgp - 2 * gp) {
+                    const double sn = sin(OC_PI / 4 * bp / (mgp / 2 - gp));
+                    W = 1.0 * sn * sn;
+                } else if (bp >= b0p + mgp - 2 * gp && bp <= b0p + OC_PI - 2 * gp) {
+                    W = 1;
+                } else if (bp > b0p + OC_PI - 2 * gp && bp <= b0p + OC_PI + mgp) {
+                    const double sn = sin(OC_PI / 4 * (OC_PI + mgp - bp) / (mgp / 2 + gp));
+                    W = 1.0 * sn * sn;
+                } else {
+                    W = 0;
+                }
+                w[g] = in[g] * dp * cos(gp) * W;
+            }
+            const double *tap = G + x * fs;
+            double *out = rcov + row * lg;
+            for (int g = 0; g < lg; ++g) {
+                double acc = 0;
+                for (int q = 0; q < lg; ++q) acc += w[q] * tap[(lg - 1) + g - q];
+                out[g] = gip * acc;
+            }
+        }
+        free(w);
+    }
+    free(G);
+}
+
+OC_API void oc_fdkui_bp(double *display, const double *rcov, const int *size, int nz, const double *beta, int nb,
+                        double D, double ds2d, const double *gama, int lg, const double *xi, int lx, int nthreads)
+{
+    set_threads(nthreads);
+    const double gint = fabs(gama[1] - gama[0]), xint = fabs(xi[1] - xi[0]);
+    const double bint = fabs(beta[1] - beta[0]);
+    const double maxg = gama[0] > gama[lg - 1] ? gama[0] : gama[lg - 1];
+    const double ming = gama[0] < gama[lg - 1] ? gama[0] : gama[lg - 1];
+    const double maxx = xi[0] > xi[lx - 1] ? xi[0] : xi[lx - 1];
+    const double minx = xi[0] < xi[lx - 1] ? xi[0] : xi[lx - 1];
+    const int nt = size[0], ns = size[1];
+    const double rz = 1.0 * size[2] / nz;
+    /* integer halves, as the reference divides its int extents (:103-105) */
+    const double ct = size[0] / 2, cs = size[1] / 2, cz = size[2] / 2;
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
+    for (int z = 0; z < nz; ++z)
+        for (int s = 0; s < ns; ++s)
+            for (int t = 0; t < nt; ++t) {
+                double acc = 0;
+                const double it = (t - 0.5) - ct, is = (s - 0.5) - cs, iz = (z - 0.5) * rz - cz;
+                for (int b = 0; b < nb; ++b) {
+                    const double bt = beta[b];
+                    const double st = D * cos(bt + OC_PI / 2), ss = D * sin(bt + OC_PI / 2), sz = 0;
+                    const double L2 = 1.0 * (it - st) * (it - st) + 1.0 * (is - ss) * (is - ss) + 1.0 * (iz - sz) * (iz - sz);
+                    const double dt = it * cos(bt) + is * sin(bt);
+                    const double ds = -it * sin(bt) + is * cos(bt);
+                    const double dz = iz;
+                    const double X = ds2d * tan(asin(dz / sqrt(L2)));
+                    const double Gm = atan(dt / (D - ds));
+                    const double pr = sqrt(L2) / sqrt(L2 - 1.0 * dz * dz);
+                    double val = 0;
+                    if (Gm >= ming && Gm < maxg && X >= minx && X < maxx) {
+                        unsigned int x1 = (unsigned int)floor(fabs(X - xi[0]) / xint), x2 = x1 + 1;
+                        unsigned int g1 = (unsigned int)floor(fabs(Gm - gama[0]) / gint), g2 = g1 + 1;
+                        if (x2 > (unsigned)(lx - 1)) { x2 = lx - 1; if (x1 > x2) x1 = x2; }   /* read-past-end guard */
+                        if (g2 > (unsigned)(lg - 1)) { g2 = lg - 1; if (g1 > g2) g1 = g2; }
+                        const double xg1 = fabs(X - xi[x1]), xg2 = fabs(xi[x2] - X);
+                        const double gg1 = fabs(Gm - gama[g1]), gg2 = fabs(gama[g2] - Gm);
+                        const double *rb = rcov + (long)b * lg * lx;
+                        val = (xg2 * gg2 * rb[(long)x1 * lg + g1] + xg1 * gg2 * rb[(long)x2 * lg + g1]
+                               + xg2 * gg1 * rb[(long)x1 * lg + g2] + xg1 * gg1 * rb[(long)x2 * lg + g2])
+                              / (gint * xint) / L2 * (bint / pr);
+                    }
+                    acc += val;
+                }
+                display[((long)z * ns + s) * nt + t] = acc;
+            }
+}
+
+/* ------------------------------------------------------------------------ */
 /* IterativeFDK error slice (IterativeFDKerrCompute.cu:12-76): for the image  */
 /* slice t, every (view, z, s) gathers, over the U samples along each ray of  */
 /* the view and every detector bin P, the weighted difference between the     */

@@ -69,6 +69,10 @@ class Oracle:
         lib.oc_cone_segments.argtypes = [_i, _i, _i, _f64p, _d, _d, _d, _f32p, _f32p, _f32p,
                                          _i, _i, _i, _d, _i, _i]
         lib.oc_cone_segments.restype = C.c_longlong
+        _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        lib.oc_fdkui_taps.argtypes = [_f64p, _d, _f64p, _i, _i, _d]
+        lib.oc_fdkui_filter.argtypes = [_f64p, _f64p, _f64p, _f64p, _f64p, _d, _d, _d, _d, _i, _i, _i, _i]
+        lib.oc_fdkui_bp.argtypes = [_f64p, _f64p, _ip, _i, _f64p, _i, _d, _d, _f64p, _i, _f64p, _i, _i]
         lib.oc_iterfdk_err.argtypes = [_f32p, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p, _i, _i, _i, _i, _i, _i,
                                        _i, _d, _i, _i]
 
@@ -232,6 +236,25 @@ class Oracle:
                            _f64(size), nt, ns, self.nthreads)
         return out
 
+    def fdkui_filter(self, R, xi, gama, beta, b0, maxg, D, ds2d):
+        """Curved-detector FDK filter stage: R [view][xi][gamma] (double) ->
+        weighted, filtered rows, same layout."""
+        R = _f64(R)
+        nb, lx, lg = R.shape
+        out = np.zeros_like(R)
+        self.lib.oc_fdkui_filter(out.ravel(), R.ravel(), _f64(xi), _f64(gama), _f64(beta), float(b0), float(maxg),
+                                 float(D), float(ds2d), lg, nb, lx, self.nthreads)
+        return out
+
+    def fdkui_bp(self, rcov, size, z_length, beta, D, ds2d, gama, xi):
+        """Curved-detector FDK backprojection: display [z][s][t] (double)."""
+        rcov = _f64(rcov)
+        size = np.ascontiguousarray(size, np.int32)
+        out = np.zeros((z_length, size[1], size[0]), np.float64)
+        self.lib.oc_fdkui_bp(out.ravel(), rcov.ravel(), size, int(z_length), _f64(beta), len(beta), float(D),
+                             float(ds2d), _f64(gama), len(gama), _f64(xi), len(xi), self.nthreads)
+        return out
+
     def iterfdk_err(self, pic, beta, U, P, G, size, D, t):
         """IterativeFDKerrCompute: error slice [beta][z][s] of image slice t
         (0-based here; the MEX gateway subtracts 1 from its MATLAB index)."""
@@ -287,6 +310,10 @@ class RefCPU:
         L["fbpfan"].ref_fbpfan_conv.argtypes = [_f32p, _f32p, _f32p, _i, _i]
         L["fbpfan"].ref_fbpfan_bp.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i, _d]
         L["fbppar"].ref_fbppar.argtypes = [_f32p, _f32p, _f32p, _f32p, _i, _i, _f64p, _i, _i]
+        _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        L["fdkui"].ref_fdkui_G.argtypes = [_f64p, _d, _f64p, _i, _d]
+        L["fdkui"].ref_fdkui_filter_rows.argtypes = [_f64p, _f64p, _f64p, _f64p, _f64p, _d, _d, _d, _d, _ip, _ip, _i]
+        L["fdkui"].ref_fdkui_bp.argtypes = [_f64p, _f64p, _ip, _i, _f64p, _i, _d, _d, _f64p, _i, _f64p, _i]
         L["iterfdk"].ref_iterfdk_err.argtypes = [_f32p, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p, _i, _i, _i, _i,
                                                  _i, _i, _i, _d, _i]
 
@@ -389,6 +416,25 @@ class RefCPU:
         out = np.zeros(shape, np.float32)
         self.libs["fbppar"].ref_fbppar(out.ravel(), _f32(R).ravel(), _f32(T), _f32(theta), len(theta), len(T),
                                        _f64(size), nt, ns)
+        return out
+
+    def fdkui_filter_rows(self, R, xi, gama, beta, b0, maxg, D, ds2d, xs, bs):
+        """PreWeightFiltration rows (xs[k], bs[k]) of R [view][80][936] (the
+        kernel's fixed launch shape); R is weighted in place, so a copy is used."""
+        R = np.array(R, np.float64, copy=True, order="C")
+        xs = np.ascontiguousarray(xs, np.int32)
+        bs = np.ascontiguousarray(bs, np.int32)
+        out = np.zeros((len(xs), R.shape[2]), np.float64)
+        self.libs["fdkui"].ref_fdkui_filter_rows(out.ravel(), R.ravel(), _f64(xi), _f64(gama), _f64(beta), float(b0),
+                                                 float(maxg), float(D), float(ds2d), xs, bs, len(xs))
+        return out
+
+    def fdkui_bp(self, rcov, size, z_length, beta, D, ds2d, gama, xi):
+        rcov = _f64(rcov)
+        size = np.ascontiguousarray(size, np.int32)
+        out = np.zeros((z_length, size[1], size[0]), np.float64)
+        self.libs["fdkui"].ref_fdkui_bp(out.ravel(), rcov.ravel(), size, int(z_length), _f64(beta), len(beta),
+                                        float(D), float(ds2d), _f64(gama), len(gama), _f64(xi), len(xi))
         return out
 
     def iterfdk_err(self, pic, beta, U, P, G, size, D, t):

@@ -113,6 +113,19 @@ def main():
     for t in (1, 10):
         out[f"ifdk_err_t{t}"] = ref.iterfdk_err(ipic, ibeta, iU, iP, iG, isize, 70.0, t)
 
+    # --- curved-detector FDK (ImplementUI.cu) ---------------------------------
+    from ctgb.geometry import curved_fdk_case
+    c = curved_fdk_case("filter")
+    Rui = np.random.default_rng(77).random((len(c["beta"]), 80, 936))
+    xs = np.array([0, 11, 39, 40, 79] * 5, np.int32)
+    bs = np.repeat(np.arange(5, dtype=np.int32), 5)
+    out["ui_filter_rows"] = ref.fdkui_filter_rows(Rui, c["xi"], c["gama"], c["beta"], c["b0"], c["maxg"], c["D"],
+                                                  c["ds2d"], xs, bs)
+    out["ui_filter_xs"], out["ui_filter_bs"] = xs, bs
+    c = curved_fdk_case("bp")
+    rc = np.random.default_rng(78).random((len(c["beta"]), len(c["xi"]), len(c["gama"]))) - 0.5
+    out["ui_bp"] = ref.fdkui_bp(rc, c["size"], c["z_length"], c["beta"], c["D"], c["ds2d"], c["gama"], c["xi"])
+
     dst = Path(__file__).resolve().parent / "reference_kernels.npz"
     if dst.exists():
         old = np.load(dst)

@@ -102,3 +102,32 @@ def test_iterative_fdk_error_matches_reference(oracle, golden, t):
     assert np.count_nonzero(ref) > ref.size // 2        # the case exercises the gathers
     assert rel_l2(out, ref) <= TOL
     assert np.mean(out == ref) > 0.99
+
+
+def test_curved_fdk_filter_rows_match_reference(oracle, golden):
+    """ImplementUI.cu PreWeightFiltration at its fixed 936 x 80 launch shape
+    (run by the checker with a real barrier per block), 25 rows over five views
+    across the Parker regions."""
+    from ctgb.geometry import curved_fdk_case
+    c = curved_fdk_case("filter")
+    R = np.random.default_rng(77).random((len(c["beta"]), 80, 936))
+    out = oracle.fdkui_filter(R, c["xi"], c["gama"], c["beta"], c["b0"], c["maxg"], c["D"], c["ds2d"])
+    rows = out[golden["ui_filter_bs"], golden["ui_filter_xs"]]
+    ref = golden["ui_filter_rows"]
+    # the first view's rows are NaN in the reference: with a symmetric detector the
+    # edge gamma is half the fan angle, (b0 + fan) - 2 gamma rounds above b0, and the
+    # Parker ramp divides by fan/2 - gamma = 0 (ImplementUI.cu:54-55)
+    nan = np.isnan(ref)
+    assert nan[:5].all() and not nan[5:].any()
+    np.testing.assert_array_equal(np.isnan(rows), nan)
+    assert rel_l2(rows[~nan], ref[~nan]) <= 1e-12
+
+
+def test_curved_fdk_bp_matches_reference(oracle, golden):
+    from ctgb.geometry import curved_fdk_case
+    c = curved_fdk_case("bp")
+    rc = np.random.default_rng(78).random((len(c["beta"]), len(c["xi"]), len(c["gama"]))) - 0.5
+    out = oracle.fdkui_bp(rc, c["size"], c["z_length"], c["beta"], c["D"], c["ds2d"], c["gama"], c["xi"])
+    ref = golden["ui_bp"]
+    assert np.count_nonzero(ref) > ref.size // 2
+    assert rel_l2(out, ref) <= 1e-12
