@@ -175,7 +175,7 @@ using namespace ct;
 struct ct_cone_plan {
     ConeGeom g{};
     DevBuf trig, vsrc, P, xi;
-    DevBuf quads, rcov, G, wtab, norms, graze, volT, pwt, win;
+    DevBuf quads, rcov, G, wtab, norms, graze, volT, pwt, win, scan;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     FilterOpts filt;
@@ -186,9 +186,34 @@ struct ct_cone_plan {
     ~ct_cone_plan() {
         trig.release(); vsrc.release(); P.release(); xi.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
-        volT.release(); pwt.release(); win.release();
+        volT.release(); pwt.release(); win.release(); scan.release();
     }
 };
+
+// CSR export shared by the cone and fan plans: count pass, grazing-list check,
+// scan, and the fill pass when arrays are given.
+template <class Launch>
+static int sysmat_common(Launch launch, DevBuf &graze, DevBuf &scan, long long nrows, long long *d_row_ptr,
+                         int *d_col, float *d_val, long long cap, long long *nnz, cudaStream_t st) {
+    CT_REQUIRE(d_row_ptr && nnz, "sysmat: null row pointer or nnz");
+    CT_REQUIRE(nrows > 0 && nrows < (1LL << 31), "sysmat: row count out of range");
+    CT_REQUIRE((d_col == nullptr) == (d_val == nullptr), "sysmat: give both d_col and d_val, or neither");
+    GrazeList gl;
+    int s;
+    if ((s = graze_list(graze, gl))) return s;
+    if ((s = launch(gl, false))) return s;
+    int ng = 0;
+    CT_CUDA(cudaMemcpyAsync(&ng, gl.count, sizeof(int), cudaMemcpyDeviceToHost, st), "graze count");
+    if ((s = csr_scan(d_row_ptr, (int)nrows, &scan.ptr, &scan.bytes, st))) return s;
+    long long total = 0;
+    CT_CUDA(cudaMemcpyAsync(&total, d_row_ptr + nrows, sizeof(long long), cudaMemcpyDeviceToHost, st), "nnz");
+    CT_CUDA(cudaStreamSynchronize(st), "sysmat sync");
+    CT_REQUIRE(ng <= gl.cap, "sysmat: more grazing rays than the re-walk list holds");
+    *nnz = total;
+    if (!d_col) return CT_OK;
+    CT_REQUIRE(cap >= total, "sysmat: d_col / d_val hold fewer entries than the matrix has");
+    return launch(gl, true);
+}
 
 static int check_domain(const float *a, int n, const char *what) {
     if (!a) { set_error(std::string(what) + ": null"); return CT_ERR_ARG; }
@@ -411,6 +436,19 @@ int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *str
     return ct_cone_fdk_bp(plan, plan->rcov.as<float>(), d_vol, stream);
 }
 
+int ct_cone_sysmat(ct_cone_plan *plan, int view0, int nviews, long long *d_row_ptr, int *d_col, float *d_val,
+                   long long cap, long long *nnz, void *stream) {
+    CT_REQUIRE(plan, "ct_cone_sysmat: null plan");
+    const ConeGeom &g = plan->g;
+    CT_REQUIRE(view0 >= 0 && nviews > 0 && view0 + nviews <= g.nb, "ct_cone_sysmat: view range out of bounds");
+    cudaStream_t st = as_stream(stream);
+    auto launch = [&](const GrazeList &gl, bool fill) {
+        return cone_sysmat_launch(g, view0, nviews, d_row_ptr, d_col, d_val, fill, gl, st);
+    };
+    return sysmat_common(launch, plan->graze, plan->scan, (long long)nviews * g.nx * g.np, d_row_ptr, d_col, d_val,
+                         cap, nnz, st);
+}
+
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream) {
     CT_REQUIRE(plan && segments, "ct_cone_count_segments: null argument");
     cudaStream_t st = as_stream(stream);
@@ -435,13 +473,13 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
 // ---------------------------------------------------------------------------
 struct ct_fan_plan {
     FanGeom g{};
-    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze, pwt, win;
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze, pwt, win, scan;
     std::vector<float> hPf, hbf;
     FilterOpts filt;
     double wsum = 0.0;
     ~ct_fan_plan() {
         trig_d.release(); Pd.release(); trig_f.release(); Pf.release();
-        G.release(); wtab.release(); rcov.release(); graze.release(); pwt.release(); win.release();
+        G.release(); wtab.release(); rcov.release(); graze.release(); pwt.release(); win.release(); scan.release();
     }
 };
 
@@ -512,6 +550,31 @@ int ct_fan_plan_create(ct_fan_plan **plan, int nt, int ns, const double *Size, c
 int ct_fan_plan_destroy(ct_fan_plan *plan) {
     delete plan;
     return CT_OK;
+}
+
+int ct_par_plan_create(ct_fan_plan **plan, int height, int width, const double *resolution, const double *thetaRange,
+                       int Ltheta, const double *t_Range, int Lt) {
+    CT_REQUIRE(resolution && resolution[0] > 0 && resolution[1] > 0, "resolution must be positive");
+    // x runs along width (resolution[1]), y along height (resolution[0]); pixel y*width + x,
+    // as ProjectionParallel_2D takes them (ProjectionParallel_2D.cpp:10-20)
+    const double size2[2] = {resolution[1] * width, resolution[0] * height};
+    int s = fan_plan_make(plan, width, height, size2, thetaRange, Ltheta, t_Range, Lt, 0.0, 1);
+    if (s) return s;
+    (*plan)->g.res[0] = resolution[1];
+    (*plan)->g.res[1] = resolution[0];
+    return CT_OK;
+}
+
+int ct_fan_sysmat(ct_fan_plan *plan, long long *d_row_ptr, int *d_col, float *d_val, long long cap, long long *nnz,
+                  void *stream) {
+    CT_REQUIRE(plan, "ct_fan_sysmat: null plan");
+    const FanGeom &g = plan->g;
+    cudaStream_t st = as_stream(stream);
+    auto launch = [&](const GrazeList &gl, bool fill) {
+        return fan_sysmat_launch(g, d_row_ptr, d_col, d_val, fill, gl, st);
+    };
+    return sysmat_common(launch, plan->graze, plan->scan, (long long)g.nb * g.np, d_row_ptr, d_col, d_val, cap, nnz,
+                         st);
 }
 
 int ct_fan_plan_set_filter(ct_fan_plan *plan, int kind, int window_len) {

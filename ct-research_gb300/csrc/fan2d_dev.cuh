@@ -29,10 +29,8 @@ namespace ct {
 
 enum { BP2_BACKPROJ = 0, BP2_FBPFAN = 1, BP2_FBPPAR = 2 };
 
-// Line integral of ray r = view * np + bin; sets `grazing` for rays the FP64
-// re-walk must redo (ref_walk.cu).
-__device__ __forceinline__ float fan_ray_value(const FanGeom &g, const float *__restrict__ img, long long r,
-                                               bool &grazing) {
+// Walk set-up of ray r = view * np + bin; false for rays that miss the image.
+__device__ __forceinline__ bool fan_ray_setup(const FanGeom &g, long long r, RayWalk &w) {
     const int p = (int)(r % g.np), v = (int)(r / g.np);
     const double2 tr = g.trig_d[v];
     const double sb = tr.x, cb = tr.y;
@@ -54,9 +52,16 @@ __device__ __forceinline__ float fan_ray_value(const FanGeom &g, const float *__
     }
     src[2] = 0.5;
     d[2] = 0.0;
+    return siddon_setup(src, d, n, res, w);
+}
+
+// Line integral of ray r = view * np + bin; sets `grazing` for rays the FP64
+// re-walk must redo (ref_walk.cu).
+__device__ __forceinline__ float fan_ray_value(const FanGeom &g, const float *__restrict__ img, long long r,
+                                               bool &grazing) {
     RayWalk w;
     grazing = false;
-    if (!siddon_setup(src, d, n, res, w)) return 0.0f;
+    if (!fan_ray_setup(g, r, w)) return 0.0f;
     grazing = w.grazing;
     return ray_integral(w, img, g.nt * g.ns - 1);
 }

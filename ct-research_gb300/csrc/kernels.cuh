@@ -65,6 +65,18 @@ int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_bp_launch(const FanGeom &g, const float *R, float *img, int wmode, const float *colsum, float eps,
                   float lambda, float lo, float hi, bool update, cudaStream_t st);
+// System-matrix export (sysmat.cu, ref_walk.cu): CSR rows of rays in
+// sinogram order, columns the voxel index; counts go to row_ptr[row + 1].
+int cone_sysmat_launch(const ConeGeom &g, int v0, int nv, long long *row_ptr, int *col, float *val, bool fill,
+                       const GrazeList &gl, cudaStream_t st);
+int fan_sysmat_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
+                      cudaStream_t st);
+int cone_sysmat_ref_launch(const ConeGeom &g, long long r0, long long *row_ptr, int *col, float *val, bool fill,
+                           const unsigned long long *list, const int *count, int cap, cudaStream_t st);
+int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill,
+                          const unsigned long long *list, const int *count, int cap, cudaStream_t st);
+// row_ptr[1..n] <- inclusive prefix sum of itself, row_ptr[0] <- 0; tmp is CUB scratch
+int csr_scan(long long *row_ptr, int n, void **tmp, size_t *tmp_bytes, cudaStream_t st);
 int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int nz, int iters, float step,
                    float eps, float lo, cudaStream_t st);
 int sq_diff_sum_launch(const float *a, const float *b, long long n, double *out, cudaStream_t st);

@@ -35,9 +35,10 @@ __device__ __forceinline__ double d2(double a0, double a1, double b0, double b1)
 }
 
 // ProjectionCone (ProjectionCone_3D.cu:25-375) for one ray; sb, cb are the
-// single-precision sin/cos of the float angle, widened.
-__device__ float cone_ray_ref(const ConeGeom &g, const float *__restrict__ vol, double sb, double cb, float P,
-                              float xi) {
+// single-precision sin/cos of the float angle, widened.  visit(voxel, length)
+// is called for every segment in walk order.
+template <class Visit>
+__device__ void cone_walk_ref(const ConeGeom &g, double sb, double cb, float P, float xi, Visit &&visit) {
     const double r1 = g.res[0], r2 = g.res[1], r3 = g.res[2], D = g.D;
     const double ct = g.size[0] / 2, cs = g.size[1] / 2, cz = g.size[2] / 2;
     const int nt = g.nt, ns = g.ns, nz = g.nz;
@@ -73,7 +74,7 @@ __device__ float cone_ray_ref(const ConeGeom &g, const float *__restrict__ vol, 
     ok[5] = ft[5] >= 0 && ft[5] <= thi && fs[5] >= 0 && fs[5] <= shi;
     int first = -1, second = -1;
     for (int f = 0; f < 6; ++f) if (ok[f]) { first = f; break; }
-    if (first < 0 || first == 5) return 0.0f;
+    if (first < 0 || first == 5) return;
     for (int f = first + 1; f < 6; ++f) if (ok[f]) { second = f; break; }
     const double T1 = ft[first], S1 = fs[first], Z1 = fz[first];
     double T2 = 0, S2 = 0, Z2 = 0;
@@ -81,7 +82,7 @@ __device__ float cone_ray_ref(const ConeGeom &g, const float *__restrict__ vol, 
     double Ts, Ss, Zs;
     if (d3(T1, S1, Z1, src_t, src_s, src_z) >= d3(T2, S2, Z2, src_t, src_s, src_z)) { Ts = T2; Ss = S2; Zs = Z2; }
     else { Ts = T1; Ss = S1; Zs = Z1; }
-    double ray = 0, tc = Ts / r1, sc = Ss / r2, zc = Zs / r3;
+    double tc = Ts / r1, sc = Ss / r2, zc = Zs / r3;
     const int up_t = (1 + sig_t) / 2, up_s = (1 + sig_s) / 2, up_z = (1 + sig_z) / 2;
     for (int i = 0; i < nt + ns + nz - 2; ++i) {
         short gt, gs, gz;
@@ -103,15 +104,22 @@ __device__ float cone_ray_ref(const ConeGeom &g, const float *__restrict__ vol, 
         const int it = (int)floor((nt_ + tc) / 2), is = (int)floor((ns_ + sc) / 2), iz = (int)floor((nz_ + zc) / 2);
         tc = nt_; sc = ns_; zc = nz_;
         if (it >= 0 && it < nt && is >= 0 && is < ns && iz >= 0 && iz < nz)
-            ray += w * vol[((long long)iz * ns + is) * nt + it];
+            visit(((long long)iz * ns + is) * nt + it, w);
         else
             break;
     }
+}
+
+__device__ float cone_ray_ref(const ConeGeom &g, const float *__restrict__ vol, double sb, double cb, float P,
+                              float xi) {
+    double ray = 0;
+    cone_walk_ref(g, sb, cb, P, xi, [&](long long i, double w) { ray += w * vol[i]; });
     return (float)ray;
 }
 
 // ProjectionFan (ProjectionFan_2D.cu:19-216): double angle and bin.
-__device__ double fan_ray_ref(const FanGeom &g, const float *__restrict__ pic, double sb, double cb, double P) {
+template <class Visit>
+__device__ void fan_walk_ref(const FanGeom &g, double sb, double cb, double P, Visit &&visit) {
     const double r1 = g.res[0], r2 = g.res[1], D = g.D;
     const int nt = g.nt, ns = g.ns;
     const double ct = g.size[0] / 2, cs = g.size[1] / 2;
@@ -132,14 +140,14 @@ __device__ double fan_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
                         ft[3] >= 0 && ft[3] <= thi};
     int first = -1, second = -1;
     for (int f = 0; f < 4; ++f) if (ok[f]) { first = f; break; }
-    if (first < 0 || first == 3) return 0.0;
+    if (first < 0 || first == 3) return;
     for (int f = first + 1; f < 4; ++f) if (ok[f]) { second = f; break; }
     const double T1 = ft[first], S1 = fs[first];
     double T2 = 0, S2 = 0;
     if (second >= 0) { T2 = ft[second]; S2 = fs[second]; }
     double Ts, Ss;
     if (d2(T1, S1, src_t, src_s) >= d2(T2, S2, src_t, src_s)) { Ts = T2; Ss = S2; } else { Ts = T1; Ss = S1; }
-    double ray = 0, tc = Ts / r1, sc = Ss / r2;
+    double tc = Ts / r1, sc = Ss / r2;
     const int up_t = (1 + sig_t) / 2, up_s = (1 + sig_s) / 2;
     for (int i = 0; i < nt + ns - 1; ++i) {
         short gt, gs;
@@ -155,15 +163,21 @@ __device__ double fan_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
         }
         const int it = (int)floor((nt_ + tc) / 2), is = (int)floor((ns_ + sc) / 2);
         tc = nt_; sc = ns_;
-        if (it >= 0 && it < nt && is >= 0 && is < ns) ray += w * pic[(long long)is * nt + it];
+        if (it >= 0 && it < nt && is >= 0 && is < ns) visit((long long)is * nt + it, w);
         else break;
     }
+}
+
+__device__ double fan_ray_ref(const FanGeom &g, const float *__restrict__ pic, double sb, double cb, double P) {
+    double ray = 0;
+    fan_walk_ref(g, sb, cb, P, [&](long long i, double w) { ray += w * pic[i]; });
     return ray;
 }
 
 // ProjectionParallel (ProjectionParallel_2D.cu:23-243); x = t axis (width),
 // y = s axis (height) of the FanGeom.
-__device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, double sb, double cb, double t) {
+template <class Visit>
+__device__ void par_walk_ref(const FanGeom &g, double sb, double cb, double t, Visit &&visit) {
     const double rx = g.res[0], ry = g.res[1], smax = g.smax;
     const int wd = g.nt, h = g.ns;
     const double cx = g.size[0] / 2, cy = g.size[1] / 2;
@@ -180,7 +194,7 @@ __device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
                         fy[3] >= 0 && fy[3] <= yhi};
     int first = -1;
     for (int f = 0; f < 4; ++f) if (ok[f]) { first = f; break; }
-    if (first < 0 || first == 3) return 0.0;
+    if (first < 0 || first == 3) return;
     const int order[3][3] = {{2, 3, 1}, {2, 3, -1}, {3, -1, -1}};
     int second = -1;
     for (int k = 0; k < 3; ++k) {
@@ -192,7 +206,7 @@ __device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
     if (second >= 0) { X2 = fx[second]; Y2 = fy[second]; }
     double Xs, Ys;
     if (d2(X1, Y1, xs, ys) >= d2(X2, Y2, xs, ys)) { Xs = X2; Ys = Y2; } else { Xs = X1; Ys = Y1; }
-    double ray = 0, xc = Xs / rx, yc = Ys / ry;
+    double xc = Xs / rx, yc = Ys / ry;
     const int up_x = (1 + sig_x) / 2, up_y = (1 + sig_y) / 2;
     for (int i = 0; i < h + wd - 1; ++i) {
         short gx, gy;
@@ -208,9 +222,14 @@ __device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
         }
         const int ix = (int)floor((nx_ + xc) / 2), iy = (int)floor((ny_ + yc) / 2);
         xc = nx_; yc = ny_;
-        if (ix >= 0 && ix < wd && iy >= 0 && iy < h) ray += w * pic[(long long)iy * wd + ix];
+        if (ix >= 0 && ix < wd && iy >= 0 && iy < h) visit((long long)iy * wd + ix, w);
         else break;
     }
+}
+
+__device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, double sb, double cb, double t) {
+    double ray = 0;
+    par_walk_ref(g, sb, cb, t, [&](long long i, double w) { ray += w * pic[i]; });
     return ray;
 }
 
@@ -285,6 +304,63 @@ fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, const float *__restric
     }
 }
 
+// One CSR row from a reference walk: pieces of zero length are dropped and
+// consecutive pieces in the same voxel merged, as the fast export does.
+struct CsrRow {
+    bool fill;
+    int *col;
+    float *val;
+    long long base;
+    int n;
+    long long prev;
+    __device__ void operator()(long long i, double w) {
+        if (!(w > 0.0)) return;
+        if (i == prev) {
+            if (fill) val[base + n - 1] += (float)w;
+            return;
+        }
+        if (fill) {
+            col[base + n] = (int)i;
+            val[base + n] = (float)w;
+        }
+        ++n;
+        prev = i;
+    }
+};
+
+// Rows of the listed (grazing) rays: counts into row_ptr[row + 1] or entries
+// at row_ptr[row]; rows are ray - r0.
+__global__ void __launch_bounds__(64)
+cone_sysmat_ref_kernel(const ConeGeom g, long long r0, long long *__restrict__ row_ptr, int *__restrict__ col,
+                       float *__restrict__ val, bool fill, const unsigned long long *__restrict__ list,
+                       const int *__restrict__ count, int cap) {
+    const int n = min(*count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long r = list[i];
+        const int p = (int)(r % g.np), x = (int)((r / g.np) % g.nx), v = (int)(r / ((unsigned long long)g.np * g.nx));
+        const long long row = (long long)r - r0;
+        const double2 tr = g.trig[v];
+        CsrRow e{fill, col, val, fill ? row_ptr[row] : 0, 0, -1};
+        cone_walk_ref(g, tr.x, tr.y, g.P[p], g.xi[x], e);
+        if (!fill) row_ptr[row + 1] = e.n;
+    }
+}
+
+__global__ void __launch_bounds__(64)
+fan_sysmat_ref_kernel(const FanGeom g, long long *__restrict__ row_ptr, int *__restrict__ col, float *__restrict__ val,
+                      bool fill, const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
+    const int n = min(*count, cap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long r = list[i];
+        const int p = (int)(r % g.np), v = (int)(r / g.np);
+        const double2 tr = g.trig_d[v];
+        CsrRow e{fill, col, val, fill ? row_ptr[r] : 0, 0, -1};
+        if (g.parallel) par_walk_ref(g, tr.x, tr.y, g.Pd[p], e);
+        else fan_walk_ref(g, tr.x, tr.y, g.Pd[p], e);
+        if (!fill) row_ptr[r + 1] = e.n;
+    }
+}
+
 }  // namespace
 
 int fan_batch_fixup_launch(const BatchSlice *d_sl, const float *img, float *out, const float *b, const float *rowsum,
@@ -311,6 +387,20 @@ int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_dou
     else
         fan_fixup_kernel<float><<<64, 64, 0, st>>>(g, img, (float *)out, b, rowsum, eps, norms, mode, list, count, cap);
     CT_LAUNCH_CHECK("fan_fixup_kernel");
+    return CT_OK;
+}
+
+int cone_sysmat_ref_launch(const ConeGeom &g, long long r0, long long *row_ptr, int *col, float *val, bool fill,
+                           const unsigned long long *list, const int *count, int cap, cudaStream_t st) {
+    cone_sysmat_ref_kernel<<<64, 64, 0, st>>>(g, r0, row_ptr, col, val, fill, list, count, cap);
+    CT_LAUNCH_CHECK("cone_sysmat_ref_kernel");
+    return CT_OK;
+}
+
+int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill,
+                          const unsigned long long *list, const int *count, int cap, cudaStream_t st) {
+    fan_sysmat_ref_kernel<<<64, 64, 0, st>>>(g, row_ptr, col, val, fill, list, count, cap);
+    CT_LAUNCH_CHECK("fan_sysmat_ref_kernel");
     return CT_OK;
 }
 

@@ -44,6 +44,9 @@ SIGNATURES = {
     "ct_cone_fdk_filter": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_fdk_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_count_segments": (_i, [_vp, C.POINTER(_ll), _vp]),
+    "ct_cone_sysmat": (_i, [_vp, _i, _i, _vp, _vp, _vp, _ll, C.POINTER(_ll), _vp]),
+    "ct_par_plan_create": (_i, [C.POINTER(_vp), _i, _i, _vp, _vp, _i, _vp, _i]),
+    "ct_fan_sysmat": (_i, [_vp, _vp, _vp, _vp, _ll, C.POINTER(_ll), _vp]),
     "ct_fan_plan_create": (_i, [C.POINTER(_vp), _i, _i, _vp, _vp, _i, _vp, _i, _d]),
     "ct_fan_plan_destroy": (_i, [_vp]),
     "ct_fan_plan_set_filter": (_i, [_vp, _i, _i]),

@@ -48,6 +48,46 @@ def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+class CsrMatrix:
+    """A projector's system matrix in CSR on the device: row_ptr int64 (rows + 1),
+    col int32, val float32 (segment lengths in mm)."""
+
+    def __init__(self, row_ptr: torch.Tensor, col: torch.Tensor, val: torch.Tensor, shape):
+        self.row_ptr, self.col, self.val, self.shape = row_ptr, col, val, tuple(shape)
+
+    @property
+    def nnz(self) -> int:
+        return int(self.val.numel())
+
+    def to_torch(self) -> torch.Tensor:
+        """torch sparse CSR tensor (int64 indices) on the same device."""
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore", UserWarning)     # torch marks sparse CSR as beta
+            return torch.sparse_csr_tensor(self.row_ptr, self.col.long(), self.val, size=self.shape)
+
+    def to_scipy(self):
+        from scipy.sparse import csr_matrix
+        return csr_matrix((self.val.cpu().numpy(), self.col.cpu().numpy(), self.row_ptr.cpu().numpy()),
+                          shape=self.shape)
+
+    def matvec(self, x: torch.Tensor) -> torch.Tensor:
+        return torch.mv(self.to_torch(), x.reshape(-1))
+
+
+def _export(fn, rows: int, cols: int, device, *head) -> CsrMatrix:
+    """Two-call CSR export of ct_*_sysmat: sizes, then entries."""
+    row_ptr = torch.empty(rows + 1, dtype=torch.int64, device=device)
+    nnz = C.c_longlong()
+    _lib.call(fn, *head, C.c_void_p(row_ptr.data_ptr()), None, None, 0, C.byref(nnz), _stream())
+    n = int(nnz.value)
+    col = torch.empty(max(n, 1), dtype=torch.int32, device=device)
+    val = torch.empty(max(n, 1), dtype=torch.float32, device=device)
+    _lib.call(fn, *head, C.c_void_p(row_ptr.data_ptr()), C.c_void_p(col.data_ptr()), C.c_void_p(val.data_ptr()),
+              n, C.byref(nnz), _stream())
+    return CsrMatrix(row_ptr, col[:n], val[:n], (rows, cols))
+
+
 class ConePlan:
     """Cone-beam operators for one ConeGeometry (ct_cone_plan_*)."""
 
@@ -128,6 +168,14 @@ class ConePlan:
         _lib.call("ct_cone_fdk_bp", self._h, _tptr(filtered), _tptr(out), _stream())
         return out
 
+    def sysmat(self, view0: int = 0, nviews: int | None = None, device="cuda") -> CsrMatrix:
+        """CSR system matrix of views view0 .. view0 + nviews - 1 (ct_cone_sysmat):
+        A vol equals fp(vol) on those views to float rounding."""
+        g = self.geom
+        nviews = len(g.beta) - view0 if nviews is None else int(nviews)
+        rows = nviews * len(g.xi) * len(g.P)
+        return _export("ct_cone_sysmat", rows, g.nt * g.ns * g.nz, device, self._h, int(view0), nviews)
+
     def count_segments(self) -> int:
         n = C.c_longlong()
         _lib.call("ct_cone_count_segments", self._h, C.byref(n), _stream())
@@ -168,6 +216,11 @@ class FanPlan:
     def new_image(self, device="cuda"):
         return torch.zeros(self.geom.img_shape, dtype=torch.float32, device=device)
 
+    def sysmat(self, device="cuda") -> CsrMatrix:
+        """CSR system matrix (ct_fan_sysmat): rows [beta][P], columns s * t_length + t."""
+        g = self.geom
+        return _export("ct_fan_sysmat", len(g.beta) * len(g.P), g.nt * g.ns, device, self._h)
+
     def new_sino(self, device="cuda"):
         return torch.zeros(self.geom.sino_shape, dtype=torch.float32, device=device)
 
@@ -198,6 +251,22 @@ class FanPlan:
         out = self.new_image(proj.device) if out is None else out
         _lib.call("ct_fan_fbp", self._h, _tptr(proj), _tptr(out), int(filter_mode), _stream())
         return out
+
+
+class ParPlan(FanPlan):
+    """2D parallel-beam operators (ct_par_plan_create: the ProjectionParallel_2D
+    geometry, image height x width, resolution = (along height, along width))."""
+
+    def __init__(self, height: int, width: int, resolution, theta, t_range):
+        res = np.ascontiguousarray(resolution, np.float64)
+        theta = np.ascontiguousarray(theta, np.float64)
+        t_range = np.ascontiguousarray(t_range, np.float64)
+        self.geom = FanGeometry(int(width), int(height), (res[1] * width, res[0] * height), theta, t_range, 0.0,
+                                "parallel")
+        self._h = C.c_void_p()
+        self._keep = (res, theta, t_range)
+        _lib.call("ct_par_plan_create", C.byref(self._h), int(height), int(width), _np_ptr(res), _np_ptr(theta),
+                  len(theta), _np_ptr(t_range), len(t_range))
 
 
 def iterfdk_err(pic: torch.Tensor, beta, U, P, G, size, D: float, t: int, out: torch.Tensor | None = None):

@@ -181,6 +181,16 @@ int ct_cone_fdk(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *str
  * already filtered sinogram. */
 int ct_cone_fdk_filter(ct_cone_plan *plan, const float *d_proj, float *d_filtered, void *stream);
 int ct_cone_fdk_bp(ct_cone_plan *plan, const float *d_filtered, float *d_vol, void *stream);
+/* The projector's system matrix as CSR (GenSysMatCircular3D.m computes it in
+ * MATLAB; no GPU counterpart in the reference).  Rows: the rays of views
+ * view0 .. view0 + nviews - 1 in sinogram order ([beta][xi][P], row 0 = the
+ * first ray of view0); columns: voxel index of the [z][s][t] volume; values:
+ * segment lengths in mm, from the forward projector's own walk, so A vol
+ * equals ct_cone_fp to float rounding.  Call with d_col = d_val = NULL to get
+ * d_row_ptr (rows + 1 int64, device) and *nnz; call again with device arrays
+ * of cap >= *nnz entries to fill them. */
+int ct_cone_sysmat(ct_cone_plan *plan, int view0, int nviews, long long *d_row_ptr, int *d_col,
+                   float *d_val, long long cap, long long *nnz, void *stream);
 /* Exact number of Siddon segments over all rays of the plan (host result). */
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream);
 
@@ -189,6 +199,15 @@ int ct_fan_plan_create(ct_fan_plan **plan, int t_length, int s_length, const dou
                        const double *BetaScanRange, int LBeta, const double *Pdomain, int LP,
                        double Distance);
 int ct_fan_plan_destroy(ct_fan_plan *plan);
+/* Parallel-beam plan (ProjectionParallel_2D geometry): image height x width,
+ * resolution[0] along the height, resolution[1] along the width; works with
+ * ct_fan_fp / ct_fan_fp_residual / ct_fan_sysmat. */
+int ct_par_plan_create(ct_fan_plan **plan, int height, int width, const double *resolution,
+                       const double *thetaRange, int Ltheta, const double *t_Range, int Lt);
+/* The 2D projector's system matrix as CSR (GenSysMatFan.m / GenSysMatParal.m
+ * compute it in MATLAB), as ct_cone_sysmat: rows [beta][P], columns s * t_length + t. */
+int ct_fan_sysmat(ct_fan_plan *plan, long long *d_row_ptr, int *d_col, float *d_val, long long cap,
+                  long long *nnz, void *stream);
 /* FBP filter options, as ct_cone_plan_set_filter / ct_cone_plan_set_short_scan. */
 int ct_fan_plan_set_filter(ct_fan_plan *plan, int kind, int window_len);
 int ct_fan_plan_set_short_scan(ct_fan_plan *plan, int enable);
