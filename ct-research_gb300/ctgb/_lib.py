@@ -72,6 +72,7 @@ SIGNATURES = {
     "ct_FDKUI": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, _i, _i, _vp, _i]),
     "ct_fdkui_filter": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _d, _d, _i, _i, _i, _vp]),
     "ct_fdkui_bp": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _d, _i, _i, _i, _vp, _i, _vp]),
+    "ct_csr_kaczmarz": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _vp]),
     "ct_tv_flow": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _vp]),
     "ct_sq_diff_sum": (_i, [_vp, _vp, _ll, _vp, _vp]),
 }

@@ -296,6 +296,16 @@ int ct_fdkui_bp(const float *d_Rcov, double *d_Display, const double *Xigamadoma
                 int LXigama, const int *Size, int z_length, void *stream);
 
 /* ===================================================================== */
+/* Row-action reconstruction on an exported system matrix                 */
+/* ===================================================================== */
+
+/* One ART (Kaczmarz) sweep over CSR rows row_begin .. row_end - 1 in order
+ * (Iterative_algorithm/ART.m:57-75): x <- x - lambda a_j (a_j.x - b_j) / (a_j.a_j),
+ * rows with a_j.a_j = 0 skipped.  CSR as ct_*_sysmat exports it; device pointers. */
+int ct_csr_kaczmarz(const long long *d_row_ptr, const int *d_col, const float *d_val, const float *d_b,
+                    float *d_x, int row_begin, int row_end, float lambda, void *stream);
+
+/* ===================================================================== */
 /* Elementwise and regulariser kernels of the SIRT(-TV) loops.            */
 /* ===================================================================== */
 
