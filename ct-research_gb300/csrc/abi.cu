@@ -175,7 +175,7 @@ using namespace ct;
 struct ct_cone_plan {
     ConeGeom g{};
     DevBuf trig, vsrc, P, xi;
-    DevBuf quads, rcov, G, wtab, norms, graze, volT, pwt, win, scan;
+    DevBuf quads, rcov, G, wtab, norms, graze, volT, volS, pwt, win, scan;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     FilterOpts filt;
@@ -186,7 +186,7 @@ struct ct_cone_plan {
     ~ct_cone_plan() {
         trig.release(); vsrc.release(); P.release(); xi.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
-        volT.release(); pwt.release(); win.release(); scan.release();
+        volT.release(); volS.release(); pwt.release(); win.release(); scan.release();
     }
 };
 
@@ -326,36 +326,49 @@ int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable) {
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
     return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
-           plan->graze.bytes + plan->volT.bytes;
+           plan->graze.bytes + plan->volT.bytes + plan->volS.bytes;
 }
 
-// The [z][t][s] copy of the volume the forward projector reads for views
-// whose detector rows run along s (plan workspace, refreshed every call).
-static int transposed_copy(ct_cone_plan *plan, const float *d_vol, float **volT, cudaStream_t st) {
-    const size_t n = (size_t)plan->g.nt * plan->g.ns * plan->g.nz;
-    int s = plan->volT.ensure(n * sizeof(float));
-    if (s) return s;
-    *volT = plan->volT.as<float>();
-    return cone_transpose_ts(plan->g, d_vol, *volT, st);
+// The two zero-padded copies of the volume the forward projector reads
+// (plan workspace, refreshed every call): [z][s][t] and [z][t][s] (for views
+// whose detector rows run along s), each with kFpPadSlices empty slices
+// before and after so that the walk needs no index clamp.
+static int fp_volumes(ct_cone_plan *plan, const float *d_vol, const float **volS, const float **volT,
+                      cudaStream_t st) {
+    const size_t slice = (size_t)plan->g.nt * plan->g.ns;
+    const size_t n = slice * plan->g.nz, pad = kFpPadSlices * slice;
+    const size_t bytes = (n + 2 * pad) * sizeof(float);
+    int s;
+    if ((s = plan->volT.ensure(bytes)) || (s = plan->volS.ensure(bytes))) return s;
+    float *t = plan->volT.as<float>(), *v = plan->volS.as<float>();
+    for (float *b : {t, v}) {
+        CT_CUDA(cudaMemsetAsync(b, 0, pad * sizeof(float), st), "pad");
+        CT_CUDA(cudaMemsetAsync(b + pad + n, 0, pad * sizeof(float), st), "pad");
+    }
+    CT_CUDA(cudaMemcpyAsync(v + pad, d_vol, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "volume copy");
+    *volS = v + pad;
+    *volT = t + pad;
+    return cone_transpose_ts(plan->g, d_vol, t + pad, st);
 }
 
 int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stream) {
     CT_REQUIRE(plan && d_vol && d_proj, "ct_cone_fp: null argument");
     GrazeList gl;
-    float *volT;
+    const float *volS, *volT;
     int s;
-    if ((s = graze_list(plan->graze, gl)) || (s = transposed_copy(plan, d_vol, &volT, as_stream(stream)))) return s;
-    return cone_fp_launch(plan->g, d_vol, volT, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl, as_stream(stream));
+    if ((s = graze_list(plan->graze, gl)) || (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream)))) return s;
+    return cone_fp_launch(plan->g, volS, volT, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl,
+                          as_stream(stream));
 }
 
 int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b, const float *d_rowsum,
                         float eps, float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(plan && d_vol && d_b && d_out && d_norms, "ct_cone_fp_residual: null argument");
     GrazeList gl;
-    float *volT;
+    const float *volS, *volT;
     int s;
-    if ((s = graze_list(plan->graze, gl)) || (s = transposed_copy(plan, d_vol, &volT, as_stream(stream)))) return s;
-    return cone_fp_launch(plan->g, d_vol, volT, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
+    if ((s = graze_list(plan->graze, gl)) || (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream)))) return s;
+    return cone_fp_launch(plan->g, volS, volT, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
 static int cone_bp_common(ct_cone_plan *plan, const float *d_proj, float *d_vol, int weighting,
@@ -456,8 +469,8 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
     if (s) return s;
     CT_CUDA(cudaMemsetAsync(plan->norms.ptr, 0, 2 * sizeof(double), st), "memset");
     GrazeList gl{};
-    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(), 2, gl,
-                            st)))
+    if ((s = cone_fp_launch(plan->g, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, plan->norms.as<double>(),
+                            2, gl, st)))
         return s;
     double h = 0;
     CT_CUDA(cudaMemcpyAsync(&h, plan->norms.ptr, sizeof(double), cudaMemcpyDeviceToHost, st), "copy");

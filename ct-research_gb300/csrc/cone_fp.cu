@@ -54,7 +54,7 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
                 const int slot = atomicAdd(gl.count, 1);
                 if (slot < gl.cap) gl.rays[slot] = (unsigned long long)o;
             }
-            const float val = hit ? ray_integral(w, use_t ? volT : vol, nmax) : 0.0f;
+            const float val = hit ? ray_integral<false>(w, use_t ? volT : vol, nmax) : 0.0f;
             if (MODE == 0) {
                 out[o] = val;
             } else {
@@ -104,8 +104,9 @@ int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStre
     return CT_OK;
 }
 
-int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, float *out, const float *b,
-                   const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
+int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const float *volU, float *out,
+                   const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
+                   cudaStream_t st) {
     dim3 block(FP_BX, FP_BY);
     dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, g.nb);
     CT_REQUIRE(g.nb <= 65535, "cone_fp: at most 65535 views per launch");
@@ -117,7 +118,7 @@ int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, float
     else
         cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0f, norms, gl);
     CT_LAUNCH_CHECK("cone_fp_kernel");
-    if (mode != 2) return cone_fixup_launch(g, vol, out, b, rowsum, eps, norms, mode, gl.rays, gl.count, gl.cap, st);
+    if (mode != 2) return cone_fixup_launch(g, volU, out, b, rowsum, eps, norms, mode, gl.rays, gl.count, gl.cap, st);
     return CT_OK;
 }
 

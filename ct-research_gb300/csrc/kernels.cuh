@@ -45,10 +45,14 @@ struct GrazeList {
     int cap;
 };
 
-// vol is [z][s][t]; volT (optional) the same volume as [z][t][s], read for
-// views whose detector rows run closer to the s axis.
-int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, float *out, const float *b,
-                   const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
+// vol is [z][s][t] and volT the same volume as [z][t][s], read for views whose
+// detector rows run closer to the s axis; both point kFpPadSlices slices into
+// zero-padded copies (the walk reads unclamped, see siddon.cuh).  volU is the
+// caller's volume, read by the FP64 re-walk of grazing rays.
+constexpr int kFpPadSlices = 4;
+int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const float *volU, float *out,
+                   const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
+                   cudaStream_t st);
 int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStream_t st);
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
                       float eps, double *norms, int mode, const unsigned long long *list, const int *count, int cap,

@@ -100,7 +100,14 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
 }
 
 // One walk step: the parameter length of the current segment and its voxel;
-// then advance to the next voxel (ties resolved t, then s, then z).
+// then advance to the next voxel (ties resolved t, then s, then z).  Every
+// next-crossing parameter is recomputed from its counter with one FMA (an
+// axis that did not advance gets its previous value back exactly), so the
+// step needs no selects.  CLAMP keeps the index inside [0, nmax] for reads
+// from unpadded arrays; without it the caller's array must extend a few
+// slices beyond both ends (a step after the last crossing moves the index by
+// one stride and reads a value weighted by a zero length).
+template <bool CLAMP = true>
 __device__ __forceinline__ void walk_step(RayWalk &w, float &acur, int nmax, float &len, int &vox) {
     const float m12 = fminf(w.n1, w.n2);
     const float m = fminf(w.n0, m12);
@@ -111,27 +118,26 @@ __device__ __forceinline__ void walk_step(RayWalk &w, float &acur, int nmax, flo
     const bool b0 = w.n0 <= m12;
     const bool b1 = !b0 && (w.n1 <= w.n2);
     const bool b2 = !b0 && !b1;
-    w.k0 += b0 ? 1.0f : 0.0f;
-    w.k1 += b1 ? 1.0f : 0.0f;
-    w.k2 += b2 ? 1.0f : 0.0f;
-    w.n0 = b0 ? fmaf(w.k0, w.d0, w.a0) : w.n0;
-    w.n1 = b1 ? fmaf(w.k1, w.d1, w.a1) : w.n1;
-    w.n2 = b2 ? fmaf(w.k2, w.d2, w.a2) : w.n2;
-    int nidx = w.idx + (b0 ? w.s0 : (b1 ? w.s1 : w.s2));
-    // keeps a read after the last crossing inside the volume allocation;
-    // such a step has zero (or float-rounding) length
-    w.idx = min(max(nidx, 0), nmax);
+    if (b0) w.k0 += 1.0f;
+    if (b1) w.k1 += 1.0f;
+    if (b2) w.k2 += 1.0f;
+    w.n0 = fmaf(w.k0, w.d0, w.a0);
+    w.n1 = fmaf(w.k1, w.d1, w.a1);
+    w.n2 = fmaf(w.k2, w.d2, w.a2);
+    const int nidx = w.idx + (b0 ? w.s0 : (b1 ? w.s1 : w.s2));
+    w.idx = CLAMP ? min(max(nidx, 0), nmax) : nidx;
 }
 
+template <bool CLAMP = true>
 __device__ __forceinline__ float ray_integral(RayWalk &w, const float *__restrict__ vol, int nmax) {
     float acc = 0.0f, acur = 0.0f;
     for (int it = 0; it < w.nseg; it += 4) {
         float l0, l1, l2, l3;
         int i0, i1, i2, i3;
-        walk_step(w, acur, nmax, l0, i0);
-        walk_step(w, acur, nmax, l1, i1);
-        walk_step(w, acur, nmax, l2, i2);
-        walk_step(w, acur, nmax, l3, i3);
+        walk_step<CLAMP>(w, acur, nmax, l0, i0);
+        walk_step<CLAMP>(w, acur, nmax, l1, i1);
+        walk_step<CLAMP>(w, acur, nmax, l2, i2);
+        walk_step<CLAMP>(w, acur, nmax, l3, i3);
         const float v0 = __ldg(vol + i0), v1 = __ldg(vol + i1);
         const float v2 = __ldg(vol + i2), v3 = __ldg(vol + i3);
         acc = fmaf(l0, v0, acc);
