@@ -300,7 +300,7 @@ def run_ours(args):
     }
     dom = "cone_fp_kernel" if t_fp >= t_bp else "cone_bp_kernel+pack_quads"
     ach = kern[dom]["achieved_gbs"]
-    tr = traffic.get(dom.split("+")[0])
+    tr = traffic.get(dom.split("+")[0]) if args.size == "full" else None
     roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "traffic": tr, "kernel": dom, "peak_source": peak_kind,
                 "pair_frac": (fp_bytes + bp_bytes) / (t_fp + t_bp) / 1e9 / peak}
