@@ -24,11 +24,14 @@ namespace {
 
 constexpr int FP_BX = 32;   // detector columns per block (one warp)
 constexpr int FP_BY = 4;    // detector rows per block
+#ifndef CT_FP_MINB
+#define CT_FP_MINB 16       // full occupancy (64 warps per SM): 32 registers, a few setup values spilled
+#endif
 
 // MODE 0: proj = A vol.  MODE 1: out = (b - A vol) * scale, norms += (|r|^2, |b|^2).
 // MODE 2: count segments into *norms (as double).
 template <int MODE>
-__global__ void __launch_bounds__(FP_BX * FP_BY)
+__global__ void __launch_bounds__(FP_BX * FP_BY, CT_FP_MINB)
 cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__restrict__ volT,
                float *__restrict__ out, const float *__restrict__ b, const float *__restrict__ rowsum, float eps,
                double *__restrict__ norms, const GrazeList gl) {

@@ -35,11 +35,16 @@ def nvcc() -> str:
     return exe
 
 
+def _env_flags() -> list[str]:
+    """Extra nvcc flags from CTGB_NVCC_FLAGS (tuning builds, e.g. -DCT_FP_MINB=9)."""
+    return os.environ.get("CTGB_NVCC_FLAGS", "").split()
+
+
 def _flags(extra: list[str] | None = None) -> list[str]:
     # host code: no FMA contraction, so host-built tables round as the oracle's on every CPU
     return ["-O3", "-std=c++17", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", f"-I{INCLUDE}",
             f"-I{CSRC}",
-            "--expt-relaxed-constexpr", *(extra or [])]
+            "--expt-relaxed-constexpr", *_env_flags(), *(extra or [])]
 
 
 def _stale() -> bool:
