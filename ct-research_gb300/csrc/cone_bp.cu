@@ -21,6 +21,8 @@
 // inside the thread with the ZC sums in registers, and each voxel is written
 // once at the end (no atomics, deterministic).  The fused SIRT variant writes
 // clamp(x + lambda * bp / (colsum + eps), lo, hi) instead of bp.
+#include <type_traits>
+
 #include "cone_geom.cuh"
 
 namespace ct {
@@ -229,40 +231,47 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         } else {
             wv = lr * lr * g.bint;
         }
-        const float c0 = 2.0f * mts;
+        // the chord factor 2 * mts folds into the detector-column weights; where
+        // a z face can limit the chord the factor becomes min(1, hz / (|iz| mts))
+        const float c0 = (WMODE == W_CHORD) ? 2.0f * mts : wv;
+        const float wa = wq0 * c0, wb = wq1 * c0;
+        // z of this thread that take this view, as a bit mask over k
+        const int klo = max(zlo - z0, 0), khi = min(((WMODE == W_FDK_STICKY) ? 0x7fff : zend) - z0, BP_ZC - 1);
+        const unsigned inmask = (klo > khi) ? 0u
+                                : ((khi >= 31 ? 0xffffffffu : ((2u << khi) - 1u)) & ~((1u << klo) - 1u));
+        auto body = [&](auto zlim) {
+            constexpr bool ZLIM = decltype(zlim)::value;
 #pragma unroll
-        for (int k = 0; k < BP_ZC; ++k) {
-            int z = z0 + k;
-            bool in = (z >= zlo) && (z <= zend);
-            float iz = fmaf((float)k, rz, iz0);
-            if (WMODE == W_FDK_STICKY) {
-                in = z >= zlo;
-                if (z > zhi) {
-                    z = zhi;
-                    iz = fmaf((float)zhi, rz, x_base);
+            for (int k = 0; k < BP_ZC; ++k) {
+                float iz = fmaf((float)k, rz, iz0);
+                if (WMODE == W_FDK_STICKY) {
+                    if (z0 + k > zhi) iz = fmaf((float)zhi, rz, x_base);
                 }
+                const float xi = iz * lr;
+                int x1 = (int)(fabsf(xi - x0s) * ixs);
+                x1 = min(max(x1, 0), g.nx - 2);
+                const float2 xd = xpair[x1];
+                const float wx1 = fabsf(xi - xd.x) * ixint;     // weight of row x1+1
+                const float wx0 = fabsf(xd.y - xi) * ixint;     // weight of row x1
+                const float4 q = __ldg(Qv + x1 * g.np);
+                const float top = fmaf(wa, q.x, wb * q.y);
+                const float bot = fmaf(wa, q.z, wb * q.w);
+                const float val = fmaf(wx0, top, wx1 * bot);
+                float w;
+                if (WMODE == W_CHORD) {
+                    // chord 2 * min(h_a / |d_a|) * |d|, d = (dt, ds, iz)
+                    const float d2 = fmaf(iz, iz, qq);
+                    const float len = d2 * rsqrtf(d2);
+                    w = ZLIM ? fminf(1.0f, hz / (fabsf(iz) * mts)) * len : len;
+                } else {
+                    w = 1.0f;
+                }
+                const bool in = (inmask >> k) & 1u;
+                acc[k] = in ? fmaf(val, w, acc[k]) : acc[k];
             }
-            const float xi = iz * lr;
-            int x1 = (int)(fabsf(xi - x0s) * ixs);
-            x1 = min(max(x1, 0), g.nx - 2);
-            const float2 xd = xpair[x1];
-            const float wx1 = fabsf(xi - xd.x) * ixint;     // weight of row x1+1
-            const float wx0 = fabsf(xd.y - xi) * ixint;     // weight of row x1
-            const float4 q = __ldg(Qv + x1 * g.np);
-            const float top = fmaf(wq0, q.x, wq1 * q.y);
-            const float bot = fmaf(wq0, q.z, wq1 * q.w);
-            const float val = fmaf(wx0, top, wx1 * bot);
-            float w;
-            if (WMODE == W_CHORD) {
-                // chord 2 * min(h_a / |d_a|) * |d|, d = (dt, ds, iz)
-                const float d2 = fmaf(iz, iz, qq);
-                const float len = d2 * rsqrtf(d2);
-                w = zlimit ? 2.0f * fminf(mts, hz / fabsf(iz)) * len : c0 * len;
-            } else {
-                w = wv;
-            }
-            acc[k] = in ? fmaf(val, w, acc[k]) : acc[k];
-        }
+        };
+        if (WMODE == W_CHORD && zlimit) body(std::true_type{});
+        else body(std::false_type{});
     }
 #pragma unroll
     for (int k = 0; k < BP_ZC; ++k) {
