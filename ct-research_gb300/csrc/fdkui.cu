@@ -23,8 +23,10 @@
 //    float pairs (~2^-46 relative per product, TwoSum accumulation), not in
 //    GB300's 1/64-rate FP64; the row goes out as float.
 //  * Backprojection: one thread per (t, s) column and 32 z, views inside.
-//    Per column-view the gamma position is computed in double (atan) since
-//    its bilinear weights are differences at the scale of dG ~ 1e-3 rad; the
+//    The row coordinates sit in shared memory.  Per
+//    column-view the offset of gamma from its detector sample is computed in
+//    double (one division, by the tangent-difference identity) since its
+//    bilinear weights are differences at the scale of dG ~ 1e-3 rad; the
 //    xi position is linear in z (tan(asin(z/sqrt(L2))) = z / sqrt(L2 - z^2),
 //    and L2 - z^2 is the in-plane distance), so the per-voxel work is FP32,
 //    accumulated in float pairs and written once as double.
@@ -125,13 +127,26 @@ fdkui_filter_kernel(const UIGeom g, const double *__restrict__ R, const double *
 // ---------------------------------------------------------------------------
 constexpr int kUIZ = 32;
 
+// a / b in double to ~4e-15 relative: the FP32 reciprocal and one Newton step
+// (the offsets it feeds need far less than a correctly rounded division)
+__device__ __forceinline__ double ratio(double a, double b) {
+    double r = (double)__frcp_rn((float)b);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+}
+
 struct UIView {
     double cb, sb, st, ss;        // cos, sin of beta; source position
 };
 
 __global__ void __launch_bounds__(128)
 fdkui_bp_kernel(const UIGeom g, const UIView *__restrict__ views, const double *__restrict__ gama,
-                const float *__restrict__ xif, const float *__restrict__ rcov, double *__restrict__ disp) {
+                const double *__restrict__ tang, const float *__restrict__ dgam, const float *__restrict__ xif,
+                const float *__restrict__ rcov, double *__restrict__ disp) {
+    // detector-row coordinate pairs (xi[x], xi[x+1]) for the row weights
+    extern __shared__ float2 xrow[];
+    for (int x = threadIdx.x + 32 * threadIdx.y; x < g.lx - 1; x += 128) xrow[x] = make_float2(xif[x], xif[x + 1]);
+    __syncthreads();
     const int t = blockIdx.x * 32 + threadIdx.x;
     const int s = blockIdx.y * 4 + threadIdx.y;
     const int z0 = blockIdx.z * kUIZ;
@@ -150,22 +165,44 @@ fdkui_bp_kernel(const UIGeom g, const UIView *__restrict__ views, const double *
     const float minx = (float)g.minx, maxx = (float)g.maxx;
     const float sx = (g.lx > 1 && xif[g.lx - 1] < xif[0]) ? -1.0f : 1.0f;
     const float cw0 = (float)(g.bint / (g.gint * g.xint));
+    const float gsc = (float)(1.0 / g.gint);
     const long long vstride = (long long)g.lx * g.lg;
     for (int v = 0; v < g.lb; ++v) {
         const UIView vw = views[v];
         const double dt = it * vw.cb + is * vw.sb;
         const double ds = -it * vw.sb + is * vw.cb;
-        const double gm = atan(dt / (g.D - ds));
+        const double den = g.D - ds;
+        // gamma = atan(dt / den).  Its bilinear weights are differences at the
+        // scale of dG, so the offset from a sample is computed in double from the
+        // tangent-difference identity: gamma - G_k = atan(u),
+        // u = (dt - T_k den) / (den + dt T_k), T_k = tan(G_k), |u| <~ dG, and
+        // atan(u) = u - u^3/3 to 1e-16.  An FP32 atan picks the cell.
+        const float gf = atanf((float)dt / (float)den);
+        int g1 = (int)floorf(fabsf(gf - (float)g.g0) * gsc);
+        g1 = min(max(g1, 0), g.lg - 2);
+        double u = ratio(dt - tang[g1] * den, den + dt * tang[g1]);
+        float dg = dgam[g1];
+        float del = (float)u;
+        del = del - del * del * del * (1.0f / 3.0f);
+        // one step to the neighbouring cell if the estimate missed
+        const float sg = dg >= 0.0f ? 1.0f : -1.0f;
+        const int step = (sg * del < 0.0f && g1 > 0) ? -1 : ((sg * del > sg * dg && g1 < g.lg - 2) ? 1 : 0);
+        if (step != 0) {
+            g1 += step;
+            u = ratio(dt - tang[g1] * den, den + dt * tang[g1]);
+            dg = dgam[g1];
+            del = (float)u;
+            del = del - del * del * del * (1.0f / 3.0f);
+        }
+        const double gm = gama[g1] + (double)del;
         if (!(gm >= g.ming && gm < g.maxg)) continue;
-        int g1 = (int)floor(fabs(gm - g.g0) / g.gint);
-        g1 = min(g1, g.lg - 2);
-        const float wg1 = (float)fabs(gm - gama[g1]), wg2 = (float)fabs(gama[g1 + 1] - gm);
-        const double ex = it - vw.st, es = is - vw.ss;
-        const float l2xy = (float)(ex * ex + es * es);
+        const float wg1 = fabsf(del), wg2 = fabsf(dg - del);
+        const float ex = (float)(it - vw.st), es = (float)(is - vw.ss);
+        const float l2xy = fmaf(ex, ex, es * es);
         const float rxy = sqrtf(l2xy);
         const float kx = (float)g.ds2d / rxy;              // xi per unit z
         const float cw = cw0 * rxy;                         // dBeta/(dG dXi) sqrt(L2xy)
-        const float *rv = rcov + (long long)v * vstride;
+        const float *rv = rcov + (long long)v * vstride + g1;
 #pragma unroll
         for (int k = 0; k < kUIZ; ++k) {
             const float iz = izs[k];
@@ -173,11 +210,11 @@ fdkui_bp_kernel(const UIGeom g, const UIView *__restrict__ views, const double *
             if (k >= nzc || !(X >= minx && X < maxx)) continue;
             int x1 = (int)floorf(fabsf(X - x0) * ixint);
             x1 = min(x1, g.lx - 2);
-            const float wx1 = sx * (X - xif[x1]), wx2 = sx * (xif[x1 + 1] - X);
-            const float *r1 = rv + (long long)x1 * g.lg + g1;
-            const float *r2 = r1 + g.lg;
-            const float val = wx2 * wg2 * __ldg(r1) + wx1 * wg2 * __ldg(r2) + wx2 * wg1 * __ldg(r1 + 1) +
-                              wx1 * wg1 * __ldg(r2 + 1);
+            const float2 xd = xrow[x1];
+            const float wx1 = sx * (X - xd.x), wx2 = sx * (xd.y - X);
+            const float *r1 = rv + x1 * g.lg, *r2 = r1 + g.lg;
+            const float val = wx2 * fmaf(wg2, __ldg(r1), wg1 * __ldg(r1 + 1)) +
+                              wx1 * fmaf(wg2, __ldg(r2), wg1 * __ldg(r2 + 1));
             const float l2 = fmaf(iz, iz, l2xy);
             const float r = rsqrtf(l2);
             const float term = val * (cw * r * r * r);      // / L2 / prop = sqrt(L2xy) / L2^1.5
@@ -198,7 +235,7 @@ fdkui_bp_kernel(const UIGeom g, const UIView *__restrict__ views, const double *
 // host
 // ---------------------------------------------------------------------------
 struct UIState {
-    DevBuf beta, gama, xi, xif, taps, views, rcov, R, disp;
+    DevBuf beta, gama, tang, dgam, xi, xif, taps, views, rcov, R, disp;
 };
 std::mutex g_ui_mutex;
 UIState &ui_state() {
@@ -271,7 +308,15 @@ int ui_upload(UIState &S, const UIGeom &g, const double *xi, const double *gama,
         vw[v] = UIView{std::cos(b), std::sin(b), g.D * std::cos(b + kPiUI / 2), g.D * std::sin(b + kPiUI / 2)};
     }
     std::vector<float2> taps = ui_taps(g, xi);
+    // per gamma sample: tan(G_k) and the cell width G_{k+1} - G_k
+    std::vector<double> tg(g.lg);
+    std::vector<float> dg(g.lg, 0.0f);
+    for (int k = 0; k < g.lg; ++k) {
+        tg[k] = std::tan(gama[k]);
+        if (k + 1 < g.lg) dg[k] = (float)(gama[k + 1] - gama[k]);
+    }
     int s;
+    if ((s = upload(S.tang, tg.data(), tg.size())) || (s = upload(S.dgam, dg.data(), dg.size()))) return s;
     if ((s = upload(S.beta, beta, (size_t)g.lb)) || (s = upload(S.gama, gama, (size_t)g.lg)) ||
         (s = upload(S.xi, xi, (size_t)g.lx)) || (s = upload(S.xif, xf.data(), xf.size())) ||
         (s = upload(S.taps, taps.data(), taps.size())) || (s = upload(S.views, vw.data(), vw.size())))
@@ -293,8 +338,11 @@ int ui_filter(UIState &S, const UIGeom &g, const double *d_R, float *d_rcov, cud
 int ui_bp(UIState &S, const UIGeom &g, const float *d_rcov, double *d_disp, cudaStream_t st) {
     dim3 grid((g.nt + 31) / 32, (g.ns + 3) / 4, (g.nz + kUIZ - 1) / kUIZ);
     CT_REQUIRE(grid.z <= 65535, "FDKUI: z_length too large");
-    fdkui_bp_kernel<<<grid, dim3(32, 4), 0, st>>>(g, S.views.as<UIView>(), S.gama.as<double>(), S.xif.as<float>(),
-                                                  d_rcov, d_disp);
+    const size_t smem = sizeof(float2) * (size_t)g.lx;
+    CT_REQUIRE(smem <= 48 * 1024, "FDKUI: at most 6144 detector rows");
+    fdkui_bp_kernel<<<grid, dim3(32, 4), smem, st>>>(g, S.views.as<UIView>(), S.gama.as<double>(),
+                                                     S.tang.as<double>(), S.dgam.as<float>(), S.xif.as<float>(),
+                                                     d_rcov, d_disp);
     CT_LAUNCH_CHECK("fdkui_bp_kernel");
     return CT_OK;
 }
