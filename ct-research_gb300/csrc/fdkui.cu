@@ -22,7 +22,7 @@
 //    yields NaN rows, reproduced).  The O(LG^2) convolution runs in FP32 on
 //    float pairs (~2^-46 relative per product, TwoSum accumulation), not in
 //    GB300's 1/64-rate FP64; the row goes out as float.
-//  * Backprojection: one thread per (t, s) column and 32 z, views inside.
+//  * Backprojection: one thread per (t, s) column and 16 z, views inside.
 //    The row coordinates sit in shared memory.  Per
 //    column-view the offset of gamma from its detector sample is computed in
 //    double (one division, by the tangent-difference identity) since its
@@ -125,7 +125,7 @@ fdkui_filter_kernel(const UIGeom g, const double *__restrict__ R, const double *
 // ---------------------------------------------------------------------------
 // backprojection
 // ---------------------------------------------------------------------------
-constexpr int kUIZ = 32;
+constexpr int kUIZ = 16;
 
 // a / b in double to ~4e-15 relative: the FP32 reciprocal and one Newton step
 // (the offsets it feeds need far less than a correctly rounded division)
