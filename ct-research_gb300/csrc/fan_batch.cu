@@ -34,7 +34,7 @@ __device__ __forceinline__ int find_slice(const BatchSlice *__restrict__ sl, int
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(512, 4)
 fan_batch_fp_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__restrict__ img,
                     float *__restrict__ out, const float *__restrict__ b, const float *__restrict__ rowsum,
                     float eps, double *__restrict__ norms, const GrazeList gl) {

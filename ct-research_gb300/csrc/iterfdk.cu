@@ -71,7 +71,7 @@ __device__ __forceinline__ bool near_int(float w, float fl, float marg) {
 }
 
 // One thread per (view, z, s) output of slice t.
-__global__ void __launch_bounds__(kIfdkBlock)
+__global__ void __launch_bounds__(kIfdkBlock, 12)
 iterfdk_kernel(const IfdkGeom g, const float *__restrict__ pic, const int *__restrict__ tab, int v0,
                const float2 *__restrict__ trig, const float *__restrict__ U, const double *__restrict__ P,
                const float *__restrict__ Pf, const float2 *__restrict__ K, const float2 *__restrict__ Gff,
