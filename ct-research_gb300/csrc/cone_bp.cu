@@ -169,6 +169,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
     const float irz = 1.0f / rz, iD = 1.0f / D;
     const long long vstride = (long long)g.nx * g.np;
     const float x0s = g.x0, ixs = ixint;
+    const float sxs = g.xsgn;   // direction of the detector-row domain
 
     float acc[BP_ZC];
 #pragma unroll
@@ -234,7 +235,12 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         // the chord factor 2 * mts folds into the detector-column weights; where
         // a z face can limit the chord the factor becomes min(1, hz / (|iz| mts))
         const float c0 = (WMODE == W_CHORD) ? 2.0f * mts : wv;
-        const float wa = wq0 * c0, wb = wq1 * c0;
+        // row weights (xi - xi[x1]) / dXi and (xi[x1+1] - xi) / dXi carry the domain
+        // direction and 1 / dXi, folded into the column weights too
+        const float cx = sxs * ixint;
+        const float wa = wq0 * c0 * cx, wb = wq1 * c0 * cx;
+        // row index |xi - xi0| / dXi = iz * ua + ub for z whose row is on the detector
+        const float ua = sxs * lr * ixs, ub = -sxs * x0s * ixs;
         // z of this thread that take this view, as a bit mask over k
         const int klo = max(zlo - z0, 0), khi = min(((WMODE == W_FDK_STICKY) ? 0x7fff : zend) - z0, BP_ZC - 1);
         const unsigned inmask = (klo > khi) ? 0u
@@ -247,16 +253,16 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
                 if (WMODE == W_FDK_STICKY) {
                     if (z0 + k > zhi) iz = fmaf((float)zhi, rz, x_base);
                 }
-                const float xi = iz * lr;
-                int x1 = (int)(fabsf(xi - x0s) * ixs);
-                x1 = min(max(x1, 0), g.nx - 2);
+                // an index outside [0, nx-2] (z off the detector, or a negative index
+                // wrapped by the unsigned compare) is clamped for the read only
+                const unsigned x1 = min((unsigned)(int)fmaf(iz, ua, ub), (unsigned)(g.nx - 2));
                 const float2 xd = xpair[x1];
-                const float wx1 = fabsf(xi - xd.x) * ixint;     // weight of row x1+1
-                const float wx0 = fabsf(xd.y - xi) * ixint;     // weight of row x1
-                const float4 q = __ldg(Qv + x1 * g.np);
+                const float e1 = fmaf(iz, lr, -xd.x);      // xi - xi[x1]: weight of row x1+1
+                const float e0 = fmaf(-iz, lr, xd.y);      // xi[x1+1] - xi: weight of row x1
+                const float4 q = __ldg(Qv + (int)x1 * g.np);
                 const float top = fmaf(wa, q.x, wb * q.y);
                 const float bot = fmaf(wa, q.z, wb * q.w);
-                const float val = fmaf(wx0, top, wx1 * bot);
+                const float val = fmaf(e0, top, e1 * bot);
                 float w;
                 if (WMODE == W_CHORD) {
                     // chord 2 * min(h_a / |d_a|) * |d|, d = (dt, ds, iz)
