@@ -22,7 +22,8 @@ LIB = LIBDIR / "libctgb.so"
 OBJDIR = LIBDIR / "obj"
 
 SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu", "ref_walk.cu", "fan_batch.cu",
-           "noalloc.cu", "iterfdk.cu", "fdkui.cu", "sysmat.cu", "solvers.cu"]
+           "noalloc.cu", "iterfdk.cu", "fdkui.cu", "sysmat.cu", "solvers.cu",
+           "unet_conv.cu", "unet_ops.cu"]
 # ref_walk.cu replays the reference's FP64 walk operation by operation: no FMA contraction
 PER_FILE_FLAGS = {"ref_walk.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

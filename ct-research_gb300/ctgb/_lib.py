@@ -75,6 +75,18 @@ SIGNATURES = {
     "ct_csr_kaczmarz": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _vp]),
     "ct_tv_flow": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _vp]),
     "ct_sq_diff_sum": (_i, [_vp, _vp, _ll, _vp, _vp]),
+    "ct_unet_conv3d": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, _vp]),
+    "ct_unet_conv3d_wgrad": (_i, [_vp, _vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
+    "ct_unet_status": (_i, [C.POINTER(_i)]),
+    "ct_unet_im2col27": (_i, [_vp, _i, _i, _i, _i, _vp, _vp]),
+    "ct_unet_pool2": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
+    "ct_unet_pool2_bwd": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _vp]),
+    "ct_unet_up2": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
+    "ct_unet_up2_bwd": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
+    "ct_unet_shift_t": (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _i, _i, _vp]),
+    "ct_unet_head": (_i, [_vp, _vp, _vp, _vp, _vp, _ll, _vp]),
+    "ct_unet_head_bwd": (_i, [_vp, _vp, _vp, _vp, _vp, _vp, _ll, _vp]),
+    "ct_unet_colsum": (_i, [_vp, _i, _ll, _vp, _vp]),
 }
 
 STATUS = {0: "CT_OK", 1: "CT_ERR_ARG", 2: "CT_ERR_OOM", 3: "CT_ERR_LAUNCH", 4: "CT_ERR_CUDA", 5: "CT_ERR_TIMEOUT"}

@@ -318,6 +318,61 @@ int ct_tv_flow(float *d_x, float *d_work, double *d_scratch, int nx, int ny, int
 /* d_norm[0] += sum((a - b)^2) over n floats (double accumulation). */
 int ct_sq_diff_sum(const float *d_a, const float *d_b, long long n, double *d_norm, void *stream);
 
+/* ===================================================================== */
+/* Learned warm start for SIRT-TV: the BF16 3D U-Net's kernels.           */
+/* No reference counterpart (the reference has no learned component); the */
+/* network feeds the SIRT-TV loop above its starting image.  Activations   */
+/* are bf16, channels-last [n][z][y][x][c]; weights bf16 [cout][taps][cin];*/
+/* sums FP32.  All pointers are device pointers, 16-byte aligned.         */
+/* ===================================================================== */
+
+/* out[v][co] = act(bias[co] + sum_tap sum_ci X[v + off(tap)][ci] W[co][tap][ci])
+ * with X = concat(x1 (c1 channels), x2 (c2 channels)) along channels, zero
+ * padding, ntaps 27 (3x3x3, tap = 9 (dz+1) + 3 (dy+1) + (dx+1)) or 1.  Output
+ * channels [0, co1) go to out1 ([v][co1]) and [co1, co1 + co2) to out2; act is
+ * ReLU when relu != 0, and an output value is zeroed where its mask (same
+ * layout as its output, may be null) is not > 0.  co1 + co2 in {32, 64, 128,
+ * 256}; c1, c2 multiples of 32; x a divisor or multiple of 128, and y, z such
+ * that 128-voxel x-y-z blocks tile the volume.  tcgen05 tensor cores. */
+int ct_unet_conv3d(const void *d_x1, int c1, const void *d_x2, int c2, int nb, int nz, int ny, int nx,
+                   const void *d_w, int ntaps, const float *d_bias, int relu, void *d_out1, int co1, void *d_out2,
+                   int co2, const void *d_mask1, const void *d_mask2, void *stream);
+/* dW[co][tap][ci] += sum_v dY[v][co] X[v + off(tap)][ci] (FP32 dW).  X is
+ * given channel-major [n][cin][z][y][x] as three copies shifted along x
+ * (d_xm[x] = X[x - 1], d_x0, d_xp[x] = X[x + 1]; ct_unet_shift_t makes them;
+ * d_xm / d_xp unused for ntaps 1); dY channel-major [n][cout][z][y][x].
+ * Split-K: one CTA per kper 32-voxel slices. */
+int ct_unet_conv3d_wgrad(const void *d_xm, const void *d_x0, const void *d_xp, int cin, const void *d_dy, int cout,
+                         int nb, int nz, int ny, int nx, int ntaps, int kper, float *d_dw, void *stream);
+/* Reads and clears the device flag of the convolutions' bounded waits:
+ * CT_ERR_TIMEOUT (flags != 0) when a wait gave up since the last call. */
+int ct_unet_status(int *flags);
+/* out[v][k] = vol[v + off(k)] (k < 27, zero outside), 0 for k = 27..31: the
+ * one-channel input as 32 channels for a 1-tap convolution. */
+int ct_unet_im2col27(const float *d_vol, int nb, int nz, int ny, int nx, void *d_out, void *stream);
+/* 2x2x2 max pooling and its gradient (to the first maximum of each window,
+ * when that maximum is > 0: the pooled tensors are ReLU outputs);
+ * nearest 2x upsampling and its gradient (sum of the 8 children).  Sizes are
+ * the coarse volume's; c a multiple of 8. */
+int ct_unet_pool2(const void *d_in, void *d_out, int c, int nb, int nz, int ny, int nx, void *stream);
+int ct_unet_pool2_bwd(const void *d_x, const void *d_y, const void *d_dy, void *d_dx, int c, int nb, int nz, int ny,
+                      int nx, void *stream);
+int ct_unet_up2(const void *d_in, void *d_out, int c, int nb, int nz, int ny, int nx, void *stream);
+int ct_unet_up2_bwd(const void *d_dout, void *d_din, int c, int nb, int nz, int ny, int nx, void *stream);
+/* Channel-major copies of a channels-last activation at channel offset coff
+ * of a ctot-channel buffer, shifted along x by -1 / 0 / +1 (null: skipped). */
+int ct_unet_shift_t(const void *d_in, int c, int nb, int nz, int ny, int nx, void *d_om, void *d_o0, void *d_op,
+                    int ctot, int coff, void *stream);
+/* Output head: out[v] = base[v] + b + sum_c w[c] f[v][c] (32 channels, FP32
+ * out; base may be null), and its gradient: df = w dout (f > 0),
+ * dw += sum_v dout f, db += sum_v dout. */
+int ct_unet_head(const void *d_f, const float *d_w, const float *d_b, const float *d_base, float *d_out,
+                 long long nvox, void *stream);
+int ct_unet_head_bwd(const float *d_dout, const void *d_f, const float *d_w, void *d_df, float *d_dw, float *d_db,
+                     long long nvox, void *stream);
+/* db[c] += sum_v dy[v][c] (bias gradient); c divides 256. */
+int ct_unet_colsum(const void *d_dy, int c, long long nvox, float *d_db, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
