@@ -401,6 +401,80 @@ def run_sirt_tv(args):
     print(json.dumps(line), flush=True)
 
 
+def run_warmstart(args):
+    """Learned warm start vs plain SIRT-TV on the sparse-view 512^3 scan (90 views
+    over 360 deg, the cone_512 detector and distances), noise-free data of a
+    12-ellipsoid phantom (seed 7; the training set used seeds 1000-2999).
+    Reference: --ref-iters iterations of SIRT-TV (ASD step, lam 1, 20 TV
+    sub-steps) from the FDK start; its final relative data residual is the
+    target.  Each learned start (network at 512^3, and at the 128^3 training
+    voxel size with the correction upsampled) runs the same loop until it reaches
+    that residual.  Times start when the FDK volume exists (both arms pay FDK)
+    and include the network's inference."""
+    import torch
+    import ctgb
+    from ctgb import unet, warmstart as ws
+    from ctgb.device import ConePlan
+    from ctgb.sirt import AsdConfig, AsdLoop
+    ctgb.load()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    n, views, iters = 512, 90, args.ref_iters
+    plan = ConePlan(ws.scan(n, views))
+    vol = ws.phantom_volume(n, 7)
+    b = plan.fp(vol)
+    fdk = plan.fdk(b)
+    net = ws.load()
+    loop = AsdLoop(plan, AsdConfig(iters=iters))
+    ref = loop.run(b, fdk, check_every=1)
+    tol = ref.residuals[-1][1]
+    plain = ws.time_to_residual(ref, tol)
+    plain_1e3 = ws.time_to_residual(ref, 1e-3)
+
+    def err(a, c):
+        return float(torch.linalg.vector_norm(a - c) / torch.linalg.vector_norm(c))
+
+    arms = {}
+    for mode, train_n in (("net_512", None), ("net_128_upsampled", 128)):
+        ws.warm_start(net, fdk, train_n)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        x0 = ws.warm_start(net, fdk, train_n)
+        e1.record()
+        torch.cuda.synchronize()
+        t_net = time.perf_counter() - t0
+        run = loop.run(b, x0, iters=iters, tol=tol, check_every=1)
+        hit = ws.time_to_residual(run, tol)
+        arms[mode] = {"network_seconds": t_net, "network_ms_device": e0.elapsed_time(e1),
+                      "start_rel_l2_vs_reference": err(x0, ref.x),
+                      "start_residual": run.residuals[0][1],
+                      "iterations": None if hit is None else hit[0],
+                      "seconds": None if hit is None else t_net + hit[1],
+                      "rel_l2_vs_reference": err(run.x, ref.x)}
+    ok = {k: v for k, v in arms.items() if v["seconds"] is not None}
+    best = min(ok, key=lambda k: ok[k]["seconds"]) if ok else None
+    flops = unet.flops_per_voxel() * n ** 3
+    t_full = arms["net_512"]["network_ms_device"] / 1e3
+    line = {"metric": "SIRT-TV wall time to the 500-iteration data residual, learned start", "unit": "s",
+            "value": None if best is None else arms[best]["seconds"], "higher_is_better": False,
+            "best_arm": best, "plain_seconds": plain[1], "plain_iterations": plain[0],
+            "speedup": None if best is None else plain[1] / arms[best]["seconds"],
+            "target_relative_residual": tol, "arms": arms,
+            "plain_reaches_1e-3": None if plain_1e3 is None else {"iterations": plain_1e3[0], "seconds": plain_1e3[1]},
+            "fdk_rel_l2_vs_reference": err(fdk, ref.x), "reference_rel_l2_vs_phantom": err(ref.x, vol),
+            "seconds_per_iteration": ref.seconds / ref.iterations,
+            "roofline": {"bound": "tensor", "kernel": "U-Net forward at 512^3 (all convolutions + pooling)",
+                         "achieved": flops / t_full / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": flops / t_full / 1e12 / bf16_peak, "peak_source": "measured bf16 burst"},
+            "dtype": "bf16 network / f32 SIRT-TV", "data": "synthetic (seeded ellipsoid phantoms, noise-free)",
+            "config": {"workload": "cone_512 geometry with 90 views; U-Net trained on 128^3 pairs of the same scan "
+                                   "(90-view FDK -> 500-iteration SIRT-TV)",
+                       "weights": str(ws.WEIGHTS.relative_to(ROOT))}}
+    print(json.dumps(line), flush=True)
+
+
 def run_fdk(args):
     """FDK of the 256^3 / 360-view / 512x384 cone scan (reference launch-order
     filter and sticky backprojection)."""
@@ -556,9 +630,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
     ap.add_argument("--size", choices=["full", "small"], default="full",
                     help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
-    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui"], default="pair",
+    ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui",
+                                           "warmstart"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
+    ap.add_argument("--ref-iters", type=int, default=500, help="reference SIRT-TV iterations (--workload warmstart)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
@@ -568,7 +644,7 @@ def main():
         run_ours(args)
     else:
         {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d,
-         "iterfdk": run_iterfdk, "fdkui": run_fdkui}[args.workload](args)
+         "iterfdk": run_iterfdk, "fdkui": run_fdkui, "warmstart": run_warmstart}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -74,6 +74,24 @@ tv_apply_kernel(float *__restrict__ x, const float *__restrict__ g, long long n,
         x[i] = fmaxf(fmaf(-scale, g[i], x[i]), lo);
 }
 
+// tv_apply_kernel with the ASD-POCS step on the device: state = (alpha, dp2, dg2)
+// with dp2 the squared size of the data step, so the RMS move of the sub-step
+// is alpha * sqrt(dp2 / n), i.e. scale = alpha * sqrt(dp2 / sum g^2).
+__global__ void __launch_bounds__(256)
+tv_apply_asd_kernel(float *__restrict__ x, const float *__restrict__ g, long long n, float lo,
+                    const double *__restrict__ sumsq, const double *__restrict__ state) {
+    const double ss = *sumsq, dp2 = state[1];
+    if (!(ss > 0.0) || !(dp2 > 0.0)) return;
+    const float scale = (float)(state[0] * sqrt(dp2 / ss));
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[i] = fmaxf(fmaf(-scale, g[i], x[i]), lo);
+}
+
+// alpha <- alpha * alpha_red when the TV phase moved x more than r_max times the data step
+__global__ void asd_alpha_kernel(double *state, float alpha_red, float r_max) {
+    if (sqrt(state[2]) > (double)r_max * sqrt(state[1])) state[0] *= (double)alpha_red;
+}
+
 __global__ void __launch_bounds__(256)
 sq_diff_kernel(const float *__restrict__ a, const float *__restrict__ b, long long n, double *__restrict__ out) {
     double s = 0.0;
@@ -104,6 +122,30 @@ int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int n
     return CT_OK;
 }
 
+int tv_flow_asd_launch(float *x, float *prev, float *work, double *scratch, double *state, int nx, int ny, int nz,
+                       int iters, float eps, float lo, float alpha_red, float r_max, cudaStream_t st) {
+    CT_REQUIRE(nx > 0 && ny > 0 && nz > 0, "tv: sizes must be positive");
+    CT_REQUIRE((long long)nx * ny * nz < (1LL << 31), "tv: volume too large");
+    const long long n = (long long)nx * ny * nz;
+    dim3 block(TV_BX, TV_BY, TV_BZ);
+    dim3 grid((nx + TV_BX - 1) / TV_BX, (ny + TV_BY - 1) / TV_BY, (nz + TV_BZ - 1) / TV_BZ);
+    const int ablocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
+    CT_CUDA(cudaMemsetAsync(state + 1, 0, 2 * sizeof(double), st), "asd memset");
+    if (int s = sq_diff_sum_launch(x, prev, n, state + 1, st)) return s;        // dp2
+    CT_CUDA(cudaMemcpyAsync(prev, x, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "asd copy");
+    for (int it = 0; it < iters; ++it) {
+        CT_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double), st), "tv memset");
+        tv_grad_kernel<<<grid, block, 0, st>>>(x, work, nx, ny, nz, eps * eps, scratch);
+        CT_LAUNCH_CHECK("tv_grad_kernel");
+        tv_apply_asd_kernel<<<ablocks, 256, 0, st>>>(x, work, n, lo, scratch, state);
+        CT_LAUNCH_CHECK("tv_apply_asd_kernel");
+    }
+    if (int s = sq_diff_sum_launch(x, prev, n, state + 2, st)) return s;        // dg2
+    asd_alpha_kernel<<<1, 1, 0, st>>>(state, alpha_red, r_max);
+    CT_LAUNCH_CHECK("asd_alpha_kernel");
+    return CT_OK;
+}
+
 int sq_diff_sum_launch(const float *a, const float *b, long long n, double *out, cudaStream_t st) {
     const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     if (blocks <= 0) return CT_OK;
@@ -121,6 +163,14 @@ int ct_tv_flow(float *d_x, float *d_work, double *d_scratch, int nx, int ny, int
     CT_REQUIRE(d_x && d_work && d_scratch, "ct_tv_flow: null argument");
     CT_REQUIRE(iters >= 0, "ct_tv_flow: negative iteration count");
     return ct::tv_flow_launch(d_x, d_work, d_scratch, nx, ny, nz, iters, step, eps, lo, ct::as_stream(stream));
+}
+
+int ct_tv_flow_asd(float *d_x, float *d_prev, float *d_work, double *d_scratch, double *d_state, int nx, int ny,
+                   int nz, int iters, float eps, float lo, float alpha_red, float r_max, void *stream) {
+    CT_REQUIRE(d_x && d_prev && d_work && d_scratch && d_state, "ct_tv_flow_asd: null argument");
+    CT_REQUIRE(iters >= 0, "ct_tv_flow_asd: negative iteration count");
+    return ct::tv_flow_asd_launch(d_x, d_prev, d_work, d_scratch, d_state, nx, ny, nz, iters, eps, lo, alpha_red, r_max,
+                                  ct::as_stream(stream));
 }
 
 int ct_sq_diff_sum(const float *d_a, const float *d_b, long long n, double *d_norm, void *stream) {

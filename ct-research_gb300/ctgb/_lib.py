@@ -75,6 +75,7 @@ SIGNATURES = {
     "ct_csr_kaczmarz": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _f, _vp]),
     "ct_tv_flow": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _vp]),
     "ct_sq_diff_sum": (_i, [_vp, _vp, _ll, _vp, _vp]),
+    "ct_tv_flow_asd": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _f, _f, _f, _f, _vp]),
     "ct_unet_conv3d": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, _vp]),
     "ct_unet_conv3d_wgrad": (_i, [_vp, _vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
     "ct_unet_status": (_i, [C.POINTER(_i)]),

@@ -324,6 +324,17 @@ def tv_flow(x: torch.Tensor, iters: int, step: float, eps: float = 1e-8, lo: flo
     return x
 
 
+def tv_flow_asd(x: torch.Tensor, prev: torch.Tensor, work: torch.Tensor, scratch: torch.Tensor, state: torch.Tensor,
+                iters: int, eps: float = 1e-8, lo: float = 0.0, alpha_red: float = 0.95, r_max: float = 0.95):
+    """The TV phase of one ASD-POCS iteration on the device (ct_tv_flow_asd);
+    prev = x before the data step on entry, x after it on return; state =
+    float64 [alpha, -, -]."""
+    nz, ny, nx = x.shape if x.dim() == 3 else (1, *x.shape)
+    _lib.call("ct_tv_flow_asd", _tptr(x), _tptr(prev), _tptr(work), _tptr(scratch), _tptr(state), nx, ny, nz,
+              int(iters), float(eps), float(lo), float(alpha_red), float(r_max), _stream())
+    return x
+
+
 def sq_diff_sum(a: torch.Tensor, b: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     out = torch.zeros(1, dtype=torch.float64, device=a.device) if out is None else out
     _lib.call("ct_sq_diff_sum", _tptr(a), _tptr(b), int(a.numel()), _tptr(out), _stream())

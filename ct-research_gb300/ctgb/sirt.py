@@ -160,6 +160,106 @@ class Sirt:
         return relative_residual(norms)
 
 
+@dataclass
+class AsdConfig:
+    """SIRT-TV with the TV step tied to the data step (ASD-POCS, Sidky and Pan
+    2008): every outer iteration runs one SIRT step, then ``tv_iters`` TV
+    sub-steps whose RMS size is alpha * rms(SIRT change); alpha shrinks by
+    ``alpha_red`` whenever the TV sub-steps moved x further than ``r_max`` times
+    the SIRT step did.  As the data step shrinks so does the regulariser, so the
+    data residual keeps falling (a fixed TV step stalls it)."""
+    iters: int = 500
+    lam: float = 1.0
+    eps: float = 1e-9
+    tv_iters: int = 20
+    alpha: float = 0.2
+    alpha_red: float = 0.95
+    r_max: float = 0.95
+    tv_eps: float = 1e-8
+    tol: float = 0.0             # stop when ||b - A x|| / ||b|| <= tol
+
+
+class AsdLoop:
+    """SIRT3D + TV (AsdConfig) on one plan.  The row / column sums depend only
+    on the geometry and are computed once; data and starting image are copied
+    into fixed buffers, so one captured CUDA graph of an iteration serves every
+    run.  The step sizes stay on the device: a run syncs only for residual
+    checks."""
+
+    def __init__(self, plan, cfg: AsdConfig | None = None, use_graph: bool = False):
+        self.plan, self.cfg = plan, cfg or AsdConfig()
+        g = plan.geom
+        dev_ = torch.device("cuda")
+        self.b = torch.zeros(g.sino_shape, dtype=torch.float32, device=dev_)
+        self.s = Sirt(plan, self.b, SirtConfig(lam=self.cfg.lam, eps=self.cfg.eps))
+        self.x = torch.zeros(g.vol_shape, dtype=torch.float32, device=dev_)
+        self.prev = torch.empty_like(self.x)
+        self.work = torch.empty_like(self.x)
+        self.scratch = torch.zeros(2, dtype=torch.float64, device=dev_)
+        self.state = torch.tensor([self.cfg.alpha, 0.0, 0.0], dtype=torch.float64, device=dev_)
+        self.graph = None
+        if use_graph:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self._step()                        # first call sets up plan workspaces
+            torch.cuda.current_stream().wait_stream(side)
+            torch.cuda.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                self._step()
+
+    def _step(self):
+        c, s = self.cfg, self.s
+        self.prev.copy_(self.x)
+        s.norms.zero_()
+        self.plan.fp_residual(self.x, self.b, s.rowsum, c.eps, out=s.e, norms=s.norms)
+        self.plan.bp_update(s.e, s.colsum, self.x, lam=c.lam, eps=c.eps, lo=0.0, hi=float("inf"))
+        if c.tv_iters > 0:
+            dev.tv_flow_asd(self.x, self.prev, self.work, self.scratch, self.state, c.tv_iters, c.tv_eps, 0.0,
+                            c.alpha_red, c.r_max)
+
+    def run(self, b: torch.Tensor, x0: torch.Tensor, iters: int | None = None, tol: float | None = None,
+            check_every: int = 1) -> SirtResult:
+        """Iterate from x0 on data b.  residuals: (k, relative data residual of
+        the x entering iteration k) at the checked iterations; times: seconds
+        from the start (after the copies in) to each check.  result.x is a
+        copy."""
+        c = self.cfg
+        iters = c.iters if iters is None else iters
+        tol = c.tol if tol is None else tol
+        self.b.copy_(b)
+        self.x.copy_(x0)
+        self.state[0] = c.alpha
+        residuals, times = [], []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it = 0
+        while it < iters:
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self._step()
+            it += 1
+            if it % check_every == 0 or it == iters:
+                r = relative_residual(self.s.norms)
+                residuals.append((it, r))
+                times.append(time.perf_counter() - t0)
+                if tol > 0 and r <= tol:
+                    break
+        torch.cuda.synchronize()
+        res = SirtResult(self.x.clone(), it, residuals, time.perf_counter() - t0)
+        res.alpha = float(self.state[0])
+        res.times = times
+        return res
+
+
+def sirt_tv_asd(plan, b: torch.Tensor, x0: torch.Tensor, cfg: AsdConfig | None = None, check_every: int = 1,
+                use_graph: bool = False) -> SirtResult:
+    """SIRT3D + TV (AsdConfig) from x0 on data b (one AsdLoop run)."""
+    return AsdLoop(plan, cfg, use_graph).run(b, x0, check_every=check_every)
+
+
 def save_checkpoint(path, x: torch.Tensor, iteration: int, residuals):
     """SIRT state (x, iteration, residual history) as an .npz, written atomically."""
     path = Path(path)

@@ -315,6 +315,15 @@ int ct_csr_kaczmarz(const long long *d_row_ptr, const int *d_col, const float *d
  * must hold nx*ny*nz floats; d_scratch 2 doubles. */
 int ct_tv_flow(float *d_x, float *d_work, double *d_scratch, int nx, int ny, int nz, int iters,
                float step, float eps, float lo, void *stream);
+/* The regularisation phase of one ASD-POCS iteration (SIRT-TV with the TV
+ * step tied to the data step), all on the device so iterations can be captured
+ * in a CUDA graph.  d_prev holds x before the data step; d_state = double[3]
+ * (alpha, scratch, scratch) with alpha carried across calls.  Computes
+ * dp = ||x - prev||, copies x to d_prev, runs `iters` TV sub-steps (as
+ * ct_tv_flow) of RMS size alpha * dp / sqrt(n), and multiplies alpha by
+ * alpha_red when the sub-steps moved x by more than r_max * dp. */
+int ct_tv_flow_asd(float *d_x, float *d_prev, float *d_work, double *d_scratch, double *d_state, int nx, int ny,
+                   int nz, int iters, float eps, float lo, float alpha_red, float r_max, void *stream);
 /* d_norm[0] += sum((a - b)^2) over n floats (double accumulation). */
 int ct_sq_diff_sum(const float *d_a, const float *d_b, long long n, double *d_norm, void *stream);
 
