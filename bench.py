@@ -475,6 +475,67 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
+def run_unet(args):
+    """The warm-start U-Net's tensor-core convolutions: each layer shape of the
+    network at 512^3 (forward), the whole forward pass at 512^3, and one training
+    step (forward + backward + Adam) at 128^3; CUDA events after a warm-up call."""
+    import torch
+    import ctgb
+    from ctgb import unet
+    ctgb.load()
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    n = 512
+    layers = []
+    g = torch.Generator(device="cuda").manual_seed(0)
+    for cin, cout, lvl in [(32, 32, 1), (64, 32, 1), (32, 64, 2), (64, 64, 2), (128, 64, 2), (64, 128, 4),
+                           (128, 128, 4), (256, 128, 4), (128, 256, 8), (256, 256, 8)]:
+        m = n // lvl
+        x = torch.randn((1, m, m, m, cin), device="cuda", generator=g).to(torch.bfloat16)
+        w = (0.05 * torch.randn((cout, 27, cin), device="cuda", generator=g)).to(torch.bfloat16)
+        ms = timed(lambda: unet.conv3d(x, w, relu=True), max(2, args.steps))
+        fl = 2.0 * m ** 3 * cin * cout * 27
+        layers.append({"in": cin, "out": cout, "size": m, "ms": ms, "tflops": fl / ms / 1e9})
+        del x, w
+    torch.cuda.empty_cache()
+    net = unet.UNet3D(seed=0)
+    x = torch.rand((1, n, n, n), device="cuda", generator=g)
+    fwd_ms = timed(lambda: net.forward(x), 2)
+    del x
+    torch.cuda.empty_cache()
+    xs = torch.rand((1, 128, 128, 128), device="cuda", generator=g)
+
+    def train_step():
+        out = net.forward(xs, keep=True)
+        net.adam_step(net.backward(2.0 * (out - xs) / out.numel()), lr=1e-6)
+
+    step_ms = timed(train_step, max(3, args.steps))
+    status = unet.status()
+    best = max(layers, key=lambda r: r["tflops"])
+    fl_net = unet.flops_per_voxel() * n ** 3
+    line = {"metric": "U-Net forward at 512^3", "value": fwd_ms, "unit": "ms", "higher_is_better": False,
+            "network_tflops": fl_net / fwd_ms / 1e9, "train_step_128_ms": step_ms, "layers": layers,
+            "roofline": {"bound": "tensor", "kernel": f"conv_fwd_kernel<{best['out']}> {best['in']}->{best['out']} "
+                                                      f"at {best['size']}^3",
+                         "achieved": best["tflops"], "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": best["tflops"] / bf16_peak, "peak_source": "measured bf16 burst"},
+            "wait_flags": status, "dtype": "bf16 (FP32 accumulate)", "data": "synthetic",
+            "config": {"workload": "warm-start U-Net (4 levels, 32 base channels, 3x3x3), batch 1"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_fdk(args):
     """FDK of the 256^3 / 360-view / 512x384 cone scan (reference launch-order
     filter and sticky backprojection)."""
@@ -631,7 +692,7 @@ def main():
     ap.add_argument("--size", choices=["full", "small"], default="full",
                     help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
     ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui",
-                                           "warmstart"], default="pair",
+                                           "warmstart", "unet"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     ap.add_argument("--ref-iters", type=int, default=500, help="reference SIRT-TV iterations (--workload warmstart)")
@@ -644,7 +705,8 @@ def main():
         run_ours(args)
     else:
         {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d,
-         "iterfdk": run_iterfdk, "fdkui": run_fdkui, "warmstart": run_warmstart}[args.workload](args)
+         "iterfdk": run_iterfdk, "fdkui": run_fdkui, "warmstart": run_warmstart,
+         "unet": run_unet}[args.workload](args)
 
 
 if __name__ == "__main__":
