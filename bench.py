@@ -497,7 +497,7 @@ def run_unet(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
-    n = 512
+    n = 512 if args.size == "full" else 128      # small: the same kernels on 128^3 (profiling case)
     layers = []
     g = torch.Generator(device="cuda").manual_seed(0)
     for cin, cout, lvl in [(32, 32, 1), (64, 32, 1), (32, 64, 2), (64, 64, 2), (128, 64, 2), (64, 128, 4),
@@ -525,7 +525,7 @@ def run_unet(args):
     status = unet.status()
     best = max(layers, key=lambda r: r["tflops"])
     fl_net = unet.flops_per_voxel() * n ** 3
-    line = {"metric": "U-Net forward at 512^3", "value": fwd_ms, "unit": "ms", "higher_is_better": False,
+    line = {"metric": f"U-Net forward at {n}^3", "value": fwd_ms, "unit": "ms", "higher_is_better": False,
             "network_tflops": fl_net / fwd_ms / 1e9, "train_step_128_ms": step_ms, "layers": layers,
             "roofline": {"bound": "tensor", "kernel": f"conv_fwd_kernel<{best['out']}> {best['in']}->{best['out']} "
                                                       f"at {best['size']}^3",
@@ -690,7 +690,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
     ap.add_argument("--size", choices=["full", "small"], default="full",
-                    help="small: 256^3 / 90 views / 384x256 profiling case of the same kernels")
+                    help="small: the profiling case of the same kernels (pair: 256^3 / 90 views / 384x256; "
+                         "unet: 128^3 layers and network)")
     ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui",
                                            "warmstart", "unet"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")

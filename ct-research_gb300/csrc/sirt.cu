@@ -37,9 +37,10 @@ tv_grad_kernel(const float *__restrict__ x, float *__restrict__ g, int nx, int n
                double *__restrict__ sumsq) {
     const int i = blockIdx.x * TV_BX + threadIdx.x;
     const int j = blockIdx.y * TV_BY + threadIdx.y;
-    const int k = blockIdx.z * TV_BZ + threadIdx.z;
     double s = 0.0;
-    if (i < nx && j < ny && k < nz) {
+    // each thread walks z with the grid's z stride, so one launch adds a few
+    // thousand block sums to *sumsq instead of one per 256 voxels
+    for (int k = blockIdx.z * TV_BZ + threadIdx.z; i < nx && j < ny && k < nz; k += gridDim.z * TV_BZ) {
         float dx, dy, dz, in;
         fdiff(x, nx, ny, nz, i, j, k, eps2, dx, dy, dz, in);
         float gv = -(dx + dy + dz) * in;
@@ -59,7 +60,7 @@ tv_grad_kernel(const float *__restrict__ x, float *__restrict__ g, int nx, int n
             gv += az * an;
         }
         g[(k * ny + j) * nx + i] = gv;
-        s = (double)gv * gv;
+        s += (double)gv * gv;
     }
     block_sum_atomic<TV_BX * TV_BY * TV_BZ / 32>(s, sumsq);
 }
@@ -102,6 +103,14 @@ sq_diff_kernel(const float *__restrict__ a, const float *__restrict__ b, long lo
     block_sum_atomic<8>(s, out);
 }
 
+// xy tiles of the volume, and z blocks up to ~16 blocks per SM in total
+dim3 tv_grid(int nx, int ny, int nz) {
+    const int gx = (nx + TV_BX - 1) / TV_BX, gy = (ny + TV_BY - 1) / TV_BY, zb = (nz + TV_BZ - 1) / TV_BZ;
+    const long long want = 16LL * sm_count();
+    const int gz = (int)std::max<long long>(1, std::min<long long>(zb, want / ((long long)gx * gy)));
+    return dim3(gx, gy, gz);
+}
+
 }  // namespace
 
 int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int nz, int iters, float step, float eps,
@@ -110,7 +119,7 @@ int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int n
     CT_REQUIRE((long long)nx * ny * nz < (1LL << 31), "tv: volume too large");
     const long long n = (long long)nx * ny * nz;
     dim3 block(TV_BX, TV_BY, TV_BZ);
-    dim3 grid((nx + TV_BX - 1) / TV_BX, (ny + TV_BY - 1) / TV_BY, (nz + TV_BZ - 1) / TV_BZ);
+    const dim3 grid = tv_grid(nx, ny, nz);
     const int ablocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     for (int it = 0; it < iters; ++it) {
         CT_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double), st), "tv memset");
@@ -128,7 +137,7 @@ int tv_flow_asd_launch(float *x, float *prev, float *work, double *scratch, doub
     CT_REQUIRE((long long)nx * ny * nz < (1LL << 31), "tv: volume too large");
     const long long n = (long long)nx * ny * nz;
     dim3 block(TV_BX, TV_BY, TV_BZ);
-    dim3 grid((nx + TV_BX - 1) / TV_BX, (ny + TV_BY - 1) / TV_BY, (nz + TV_BZ - 1) / TV_BZ);
+    const dim3 grid = tv_grid(nx, ny, nz);
     const int ablocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     CT_CUDA(cudaMemsetAsync(state + 1, 0, 2 * sizeof(double), st), "asd memset");
     if (int s = sq_diff_sum_launch(x, prev, n, state + 1, st)) return s;        // dp2
