@@ -156,6 +156,10 @@ def test_tv_flow_matches_oracle():
     img = x[3]
     out2 = tv_flow(torch.from_numpy(img.copy()).cuda(), 3, 1e-3).cpu().numpy()
     assert rel_l2(out2 - img, tv_ref(img, 3, 1e-3) - img) <= 1e-4
+    # a volume with more z blocks than the launch holds: threads walk z with the grid's stride
+    big = np.clip(0.5 + 0.2 * rng.normal(size=(128, 160, 96)), 0, None).astype(np.float32)
+    out3 = tv_flow(torch.from_numpy(big).cuda(), 2, 1e-3, 1e-8, 0.0).cpu().numpy()
+    assert rel_l2(out3 - big, tv_ref(big, 2, 1e-3, 1e-8, 0.0) - big) <= 1e-4
 
 
 @pytest.mark.gpu
