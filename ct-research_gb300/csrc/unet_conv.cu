@@ -201,34 +201,48 @@ __device__ __forceinline__ void fail(Ctrl *c, int code) {
 
 __device__ __forceinline__ bool aborted(Ctrl *c) { return *reinterpret_cast<volatile int *>(&c->abort) != 0; }
 
-// After an abort: wait (bounded) for the loads issued into each stage.
+// After an abort: wait (bounded) for the loads issued into each of the S stages.
+template <int S>
 __device__ void drain_loads(Ctrl *c, int issued) {
-    for (int s = 0; s < kStages && s < issued; ++s) {
-        const int last = (issued - 1 - s) / kStages;   // use index of the last load into stage s
+    for (int s = 0; s < S && s < issued; ++s) {
+        const int last = (issued - 1 - s) / S;   // use index of the last load into stage s
         mbar_wait(&c->full[s], static_cast<uint32_t>(last & 1));
     }
 }
 
-// The MMA side of one CTA: K steps of two 128 x N x 16 instructions.
-template <int N>
+// The MMA side of one CTA over an S-stage ring of (A_BYTES of A, NG * N rows
+// of B) stages: per K step, NG groups of two 128 x N x 16 instructions, group g
+// reading A from byte offset g * A_STEP and the g-th B tile.
+template <int N, int S, uint32_t A_BYTES, int NG, uint32_t A_STEP>
 __device__ __forceinline__ void mma_loop(Ctrl *c, uint8_t *ring, uint32_t tmem, int ksteps) {
-    constexpr uint32_t stage = kABytes + N * kRowBytes;
+    constexpr uint32_t stage = A_BYTES + NG * N * kRowBytes;
     constexpr uint32_t idesc = idesc_bf16(kTileM, N);
     for (int k = 0; k < ksteps; ++k) {
-        const int s = k % kStages;
+        const int s = k % S;
         if (aborted(c)) break;
-        if (!mbar_wait(&c->full[s], static_cast<uint32_t>((k / kStages) & 1))) {
+        if (!mbar_wait(&c->full[s], static_cast<uint32_t>((k / S) & 1))) {
             fail(c, 2);
             break;
         }
         tc_fence_after();
-        const uint32_t sa = smem_u32(ring + s * stage), sb = sa + kABytes;
+        const uint32_t sa = smem_u32(ring + s * stage), sb = sa + A_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < 2; ++kk) umma_bf16(tmem, sw64_desc(sa + kk * 32), sw64_desc(sb + kk * 32), idesc, k | kk);
+        for (int g = 0; g < NG; ++g)
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk)
+                umma_bf16(tmem, sw64_desc(sa + g * A_STEP + kk * 32), sw64_desc(sb + g * N * kRowBytes + kk * 32), idesc,
+                          k | g | kk);
         umma_commit(&c->empty[s]);
     }
     umma_commit(&c->done);
 }
+
+// y-halo mode of the forward kernel: 8 x 16 voxel tiles of one slice; one box of
+// 8 x 18 voxels per (dz, dx, channel chunk) serves the three dy taps, whose A
+// operands start 0, 8 and 16 rows (512-byte swizzle atoms) into it.
+constexpr int kYBx = 8, kYBy = 16;
+constexpr uint32_t kYABytes = kYBx * (kYBy + 2) * kRowBytes;
+constexpr int kYStages = 3;
 
 struct FwdArgs {
     int c1, c2;              // channels of input 1 and input 2 (0: one input)
@@ -243,14 +257,17 @@ struct FwdArgs {
     const __nv_bfloat16 *mask1, *mask2;   // ReLU-derivative masks (same layout as out1 / out2) or null
 };
 
-template <int N>
+template <int N, bool YR>
 __global__ void __launch_bounds__(128, 1)
 conv_fwd_kernel(const __grid_constant__ CUtensorMap mx1, const __grid_constant__ CUtensorMap mx2,
                 const __grid_constant__ CUtensorMap mw, const FwdArgs a) {
-    constexpr uint32_t stage = kABytes + N * kRowBytes;
+    constexpr int S = YR ? kYStages : kStages;
+    constexpr uint32_t a_bytes = YR ? kYABytes : kABytes;
+    constexpr int ng = YR ? 3 : 1;
+    constexpr uint32_t stage = a_bytes + ng * N * kRowBytes;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *ring = align1024(smem_raw);
-    Ctrl *c = reinterpret_cast<Ctrl *>(ring + kStages * stage);
+    Ctrl *c = reinterpret_cast<Ctrl *>(ring + S * stage);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     int t = blockIdx.x;
@@ -262,7 +279,7 @@ conv_fwd_kernel(const __grid_constant__ CUtensorMap mx1, const __grid_constant__
     const int z0 = (t % tz) * a.bz, n0 = t / tz;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&c->full[s], 1);
             mbar_init(&c->empty[s], 1);
         }
@@ -280,27 +297,41 @@ conv_fwd_kernel(const __grid_constant__ CUtensorMap mx1, const __grid_constant__
         const int nch = (a.c1 + a.c2) / 32;
         int issued = 0;
         for (int k = 0; k < a.ksteps; ++k) {
-            const int s = k % kStages;
+            const int s = k % S;
             if (aborted(c)) break;
-            if (k >= kStages && !mbar_wait(&c->empty[s], static_cast<uint32_t>((k / kStages - 1) & 1))) {
+            if (k >= S && !mbar_wait(&c->empty[s], static_cast<uint32_t>((k / S - 1) & 1))) {
                 fail(c, 1);
                 break;
             }
-            const int tap = k / nch, ch = (k % nch) * 32;
+            // K order: (tap or (dz, dx) group) major, 32-channel chunks inner
+            const int grp = k / nch, ch = (k % nch) * 32;
             int dz, dy, dx;
-            tap_offsets(tap, a.ntaps, dz, dy, dx);
+            if (YR) {
+                dz = grp / 3 - 1;
+                dx = grp % 3 - 1;
+                dy = -1;                          // the box starts one row above the tile
+            } else {
+                tap_offsets(grp, a.ntaps, dz, dy, dx);
+            }
             uint8_t *sa = ring + s * stage;
             mbar_expect_tx(&c->full[s], stage);
             if (ch < a.c1)
                 tma_load5(sa, &mx1, &c->full[s], ch, x0 + dx, y0 + dy, z0 + dz, n0);
             else
                 tma_load5(sa, &mx2, &c->full[s], ch - a.c1, x0 + dx, y0 + dy, z0 + dz, n0);
-            tma_load3(sa + kABytes, &mw, &c->full[s], ch, tap, 0);
+            if (YR) {
+#pragma unroll
+                for (int g = 0; g < 3; ++g)                 // dy = g - 1
+                    tma_load3(sa + a_bytes + g * N * kRowBytes, &mw, &c->full[s], ch, (dz + 1) * 9 + g * 3 + (dx + 1),
+                              0);
+            } else {
+                tma_load3(sa + a_bytes, &mw, &c->full[s], ch, grp, 0);
+            }
             ++issued;
         }
-        if (aborted(c)) drain_loads(c, issued);
+        if (aborted(c)) drain_loads<S>(c, issued);
     } else if (threadIdx.x == 32) {
-        mma_loop<N>(c, ring, tmem, a.ksteps);
+        mma_loop<N, S, a_bytes, ng, kYBx * kRowBytes>(c, ring, tmem, a.ksteps);
     }
     __syncwarp();
 
@@ -426,9 +457,9 @@ conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant
             tma_load4(sa + kABytes, &mdy, &c->full[s], p, z, 0, n);
             ++issued;
         }
-        if (aborted(c)) drain_loads(c, issued);
+        if (aborted(c)) drain_loads<kStages>(c, issued);
     } else if (threadIdx.x == 32) {
-        mma_loop<N>(c, ring, tmem, ksteps);
+        mma_loop<N, kStages, kABytes, 1, 0>(c, ring, tmem, ksteps);
     }
     __syncwarp();
 
@@ -517,22 +548,29 @@ int map_ncdhw(CUtensorMap *m, const void *p, int c, int nxy, int nz, int nb, int
     return make_map(m, p, 4, dims, st, box);
 }
 
+// Dynamic shared memory of a ring (plus alignment slack and the control block).
+// Every size here keeps the CTAs an SM can hold at <= 512 TMEM columns in total.
 template <int N>
 size_t ring_smem() {
     return 1024 + kStages * (kABytes + N * kRowBytes) + sizeof(Ctrl);
 }
 
 template <int N>
+size_t yring_smem() {
+    return 1024 + kYStages * (kYABytes + 3 * N * kRowBytes) + sizeof(Ctrl);
+}
+
+template <int N, bool YR>
 int launch_fwd(const CUtensorMap &m1, const CUtensorMap &m2, const CUtensorMap &mw, const FwdArgs &a, int tiles,
                cudaStream_t st) {
-    const size_t smem = ring_smem<N>();
+    const size_t smem = YR ? yring_smem<N>() : ring_smem<N>();
     static bool attr = false;
     if (!attr) {
-        CT_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        CT_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<N, YR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "conv_fwd smem");
         attr = true;
     }
-    conv_fwd_kernel<N><<<tiles, 128, smem, st>>>(m1, m2, mw, a);
+    conv_fwd_kernel<N, YR><<<tiles, 128, smem, st>>>(m1, m2, mw, a);
     CT_LAUNCH_CHECK("conv_fwd_kernel");
     return CT_OK;
 }
@@ -575,12 +613,21 @@ int ct_unet_conv3d(const void *x1, int c1, const void *x2, int c2, int nb, int n
     CT_REQUIRE(valid_n(n) && co1 > 0 && co1 % 16 == 0 && co2 % 16 == 0 && (co2 == 0 || out2),
                "conv3d: output channels must total 32, 64, 128 or 256, split at a multiple of 16");
     CT_REQUIRE(nb > 0 && nz > 0 && ny > 0 && nx > 0, "conv3d: empty volume");
-    const int bx = nx >= 128 ? 128 : nx;
-    CT_REQUIRE(128 % bx == 0 && nx % bx == 0, "conv3d: x must be a divisor or a multiple of 128");
-    const int by = ny >= 128 / bx ? 128 / bx : ny;
-    CT_REQUIRE((128 / bx) % by == 0 && ny % by == 0, "conv3d: y must fit the 128-voxel tile");
-    const int bz = 128 / (bx * by);
-    CT_REQUIRE(nz % bz == 0, "conv3d: z must be a multiple of 128 / (x * y) for small slices");
+    // y-halo tiles (8 x 16 voxels, the three dy taps from one box) where they fit
+    const bool yr = ntaps == 27 && n <= 128 && nx % kYBx == 0 && ny % kYBy == 0;
+    int bx, by, bz;
+    if (yr) {
+        bx = kYBx;
+        by = kYBy;
+        bz = 1;
+    } else {
+        bx = nx >= 128 ? 128 : nx;
+        CT_REQUIRE(128 % bx == 0 && nx % bx == 0, "conv3d: x must be a divisor or a multiple of 128");
+        by = ny >= 128 / bx ? 128 / bx : ny;
+        CT_REQUIRE((128 / bx) % by == 0 && ny % by == 0, "conv3d: y must fit the 128-voxel tile");
+        bz = 128 / (bx * by);
+        CT_REQUIRE(nz % bz == 0, "conv3d: z must be a multiple of 128 / (x * y) for small slices");
+    }
     CT_REQUIRE(aligned16(x1) && aligned16(w) && aligned16(out1) && (!x2 || aligned16(x2)) &&
                    (!out2 || aligned16(out2)) && (!mask1 || aligned16(mask1)) && (!mask2 || aligned16(mask2)),
                "conv3d: pointers must be 16-byte aligned");
@@ -588,8 +635,9 @@ int ct_unet_conv3d(const void *x1, int c1, const void *x2, int c2, int nb, int n
     CT_REQUIRE(tiles < (1ll << 31), "conv3d: too many tiles");
     CUtensorMap m1, m2, mw;
     int s;
-    if ((s = map_ndhwc(&m1, x1, c1, nx, ny, nz, nb, bx, by, bz))) return s;
-    if ((s = map_ndhwc(&m2, c2 ? x2 : x1, c2 ? c2 : c1, nx, ny, nz, nb, bx, by, bz))) return s;
+    const int box_y = yr ? by + 2 : by;
+    if ((s = map_ndhwc(&m1, x1, c1, nx, ny, nz, nb, bx, box_y, bz))) return s;
+    if ((s = map_ndhwc(&m2, c2 ? x2 : x1, c2 ? c2 : c1, nx, ny, nz, nb, bx, box_y, bz))) return s;
     {
         const int cin = c1 + c2;
         const uint64_t dims[3] = {(uint64_t)cin, (uint64_t)ntaps, (uint64_t)n};
@@ -607,7 +655,7 @@ int ct_unet_conv3d(const void *x1, int c1, const void *x2, int c2, int nb, int n
     a.bx = bx;
     a.by = by;
     a.bz = bz;
-    a.ksteps = ntaps * (c1 + c2) / 32;
+    a.ksteps = (yr ? 9 : ntaps) * (c1 + c2) / 32;
     a.bias = bias;
     a.relu = relu;
     a.out1 = static_cast<__nv_bfloat16 *>(out1);
@@ -617,11 +665,18 @@ int ct_unet_conv3d(const void *x1, int c1, const void *x2, int c2, int nb, int n
     a.mask1 = static_cast<const __nv_bfloat16 *>(mask1);
     a.mask2 = static_cast<const __nv_bfloat16 *>(mask2);
     cudaStream_t st = as_stream(stream);
+    if (yr) {
+        switch (n) {
+            case 32: return launch_fwd<32, true>(m1, m2, mw, a, (int)tiles, st);
+            case 64: return launch_fwd<64, true>(m1, m2, mw, a, (int)tiles, st);
+            default: return launch_fwd<128, true>(m1, m2, mw, a, (int)tiles, st);
+        }
+    }
     switch (n) {
-        case 32: return launch_fwd<32>(m1, m2, mw, a, (int)tiles, st);
-        case 64: return launch_fwd<64>(m1, m2, mw, a, (int)tiles, st);
-        case 128: return launch_fwd<128>(m1, m2, mw, a, (int)tiles, st);
-        default: return launch_fwd<256>(m1, m2, mw, a, (int)tiles, st);
+        case 32: return launch_fwd<32, false>(m1, m2, mw, a, (int)tiles, st);
+        case 64: return launch_fwd<64, false>(m1, m2, mw, a, (int)tiles, st);
+        case 128: return launch_fwd<128, false>(m1, m2, mw, a, (int)tiles, st);
+        default: return launch_fwd<256, false>(m1, m2, mw, a, (int)tiles, st);
     }
 }
 

@@ -64,6 +64,10 @@ FWD_CASES = [
     (128, 0, 32, 27, 1, 2, 2, 256, None, True),
     (32, 32, 64, 27, 1, 5, 16, 16, 32, True),
     (64, 0, 128, 27, 1, 8, 4, 8, None, False),       # 128-voxel tiles spanning 4 slices
+    # y-halo tiles (x a multiple of 8, y of 16, <= 128 outputs): one box per (dz, dx) for 3 dy taps
+    (64, 0, 128, 27, 2, 3, 32, 24, None, False),
+    (32, 0, 32, 27, 1, 2, 48, 8, None, True),
+    (128, 128, 128, 27, 1, 2, 16, 16, 96, True),
 ]
 
 
