@@ -15,10 +15,11 @@
 //   adds the bias, applies ReLU or the ReLU-derivative mask of a saved
 //   activation, rounds to bf16 and splits the channels over one or two outputs.
 // * conv_wgrad_kernel (weight gradient): rows = (tap, input channel), columns
-//   = output channels, K = voxels.  Activations and output gradients are read
-//   channel-major [n][c][z][y*x]; x offsets come from three x-shifted copies
-//   (so every TMA box starts on a 64-byte boundary), y and z offsets move the
-//   box.  Split-K over voxel ranges; partial sums are added to an FP32
+//   = output channels, K = voxels in 64-voxel slices (128-byte rows, 128-byte
+//   swizzle).  Activations and output gradients are read channel-major
+//   [n][c][z][y*x]; x offsets come from three x-shifted copies (so the
+//   innermost TMA coordinate stays on the 16-byte grid), y and z offsets move
+//   the box.  Split-K over voxel ranges; partial sums are added to an FP32
 //   gradient with atomics.
 //
 // A warp-specialised pipeline per CTA: thread 0 issues TMA loads into a
@@ -123,6 +124,17 @@ __device__ __forceinline__ uint64_t sw64_desc(uint32_t saddr) {
     return d;
 }
 
+// The same for the 128-byte swizzle layout: 128-byte rows, 8-row atoms of
+// 1024 bytes, layout code 2.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(1) << 16;
+    d |= static_cast<uint64_t>(1024 >> 4) << 32;
+    d |= static_cast<uint64_t>(1) << 46;
+    d |= static_cast<uint64_t>(2) << 61;
+    return d;
+}
+
 // Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M x N.
 __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
@@ -211,12 +223,14 @@ __device__ void drain_loads(Ctrl *c, int issued) {
 }
 
 // The MMA side of one CTA over an S-stage ring of (A_BYTES of A, NG * N rows
-// of B) stages: per K step, NG groups of two 128 x N x 16 instructions, group g
-// reading A from byte offset g * A_STEP and the g-th B tile.
-template <int N, int S, uint32_t A_BYTES, int NG, uint32_t A_STEP>
+// of B) stages with ROWB-byte rows (64: 64-byte swizzle, 128: 128-byte
+// swizzle): per K step, NG groups of ROWB / 32 instructions of 128 x N x 16,
+// group g reading A from byte offset g * A_STEP and the g-th B tile.
+template <int N, int S, uint32_t A_BYTES, int NG, uint32_t A_STEP, int ROWB = kRowBytes>
 __device__ __forceinline__ void mma_loop(Ctrl *c, uint8_t *ring, uint32_t tmem, int ksteps) {
-    constexpr uint32_t stage = A_BYTES + NG * N * kRowBytes;
+    constexpr uint32_t stage = A_BYTES + NG * N * ROWB;
     constexpr uint32_t idesc = idesc_bf16(kTileM, N);
+    constexpr int KK = ROWB / 32;
     for (int k = 0; k < ksteps; ++k) {
         const int s = k % S;
         if (aborted(c)) break;
@@ -229,9 +243,12 @@ __device__ __forceinline__ void mma_loop(Ctrl *c, uint8_t *ring, uint32_t tmem, 
 #pragma unroll
         for (int g = 0; g < NG; ++g)
 #pragma unroll
-            for (int kk = 0; kk < 2; ++kk)
-                umma_bf16(tmem, sw64_desc(sa + g * A_STEP + kk * 32), sw64_desc(sb + g * N * kRowBytes + kk * 32), idesc,
-                          k | g | kk);
+            for (int kk = 0; kk < KK; ++kk) {
+                const uint32_t ao = sa + g * A_STEP + kk * 32, bo = sb + g * N * ROWB + kk * 32;
+                const uint64_t ad = ROWB == 128 ? sw128_desc(ao) : sw64_desc(ao);
+                const uint64_t bd = ROWB == 128 ? sw128_desc(bo) : sw64_desc(bo);
+                umma_bf16(tmem, ad, bd, idesc, k | g | kk);
+            }
         umma_commit(&c->empty[s]);
     }
     umma_commit(&c->done);
@@ -243,6 +260,11 @@ __device__ __forceinline__ void mma_loop(Ctrl *c, uint8_t *ring, uint32_t tmem, 
 constexpr int kYBx = 8, kYBy = 16;
 constexpr uint32_t kYABytes = kYBx * (kYBy + 2) * kRowBytes;
 constexpr int kYStages = 3;
+
+// weight-gradient ring: K slices of 64 voxels (128-byte rows, 128-byte swizzle)
+constexpr int kWK = 64;
+constexpr int kWRowBytes = 2 * kWK;
+constexpr int kWStages = 3;
 
 struct FwdArgs {
     int c1, c2;              // channels of input 1 and input 2 (0: one input)
@@ -395,7 +417,8 @@ struct WgradArgs {
     int cin, ntaps;
     int rows_per_tap, taps_per_tile, cblocks;
     int nxy, nx, nz;         // y*x plane size, x size, slices
-    long long kchunks;       // 32-voxel K slices over all samples
+    long long kchunks;       // 64-voxel K slices over all samples
+    int pchunks;             // 64-voxel slices per y*x plane (the last may run past the plane: zero fill)
     int kper;                // K slices per CTA
     float *dw;               // [N][ntaps][cin], FP32, accumulated
 };
@@ -405,10 +428,11 @@ __global__ void __launch_bounds__(128, 1)
 conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant__ CUtensorMap mx0,
                   const __grid_constant__ CUtensorMap mxp, const __grid_constant__ CUtensorMap mdy,
                   const WgradArgs a) {
-    constexpr uint32_t stage = kABytes + N * kRowBytes;
+    constexpr uint32_t a_bytes = kTileM * kWRowBytes;
+    constexpr uint32_t stage = a_bytes + N * kWRowBytes;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *ring = align1024(smem_raw);
-    Ctrl *c = reinterpret_cast<Ctrl *>(ring + kStages * stage);
+    Ctrl *c = reinterpret_cast<Ctrl *>(ring + kWStages * stage);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     const int tgroup = blockIdx.x / a.cblocks, cb = blockIdx.x % a.cblocks;
@@ -417,7 +441,7 @@ conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant
     const int ksteps = static_cast<int>(min(static_cast<long long>(a.kper), a.kchunks - k0));
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < kWStages; ++s) {
             mbar_init(&c->full[s], 1);
             mbar_init(&c->empty[s], 1);
         }
@@ -432,17 +456,17 @@ conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant
     const uint32_t tmem = c->tmem;
 
     if (threadIdx.x == 0) {
-        const int pchunks = a.nxy / 32;
+        const int pchunks = a.pchunks;
         int issued = 0;
         for (int k = 0; k < ksteps; ++k) {
-            const int s = k % kStages;
+            const int s = k % kWStages;
             if (aborted(c)) break;
-            if (k >= kStages && !mbar_wait(&c->empty[s], static_cast<uint32_t>((k / kStages - 1) & 1))) {
+            if (k >= kWStages && !mbar_wait(&c->empty[s], static_cast<uint32_t>((k / kWStages - 1) & 1))) {
                 fail(c, 1);
                 break;
             }
             long long q = k0 + k;
-            const int p = static_cast<int>(q % pchunks) * 32;
+            const int p = static_cast<int>(q % pchunks) * kWK;
             q /= pchunks;
             const int z = static_cast<int>(q % a.nz), n = static_cast<int>(q / a.nz);
             uint8_t *sa = ring + s * stage;
@@ -452,14 +476,14 @@ conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant
                 int dz, dy, dx;
                 tap_offsets(tap, a.ntaps, dz, dy, dx);
                 const CUtensorMap *m = dx < 0 ? &mxm : (dx > 0 ? &mxp : &mx0);
-                tma_load4(sa + j * a.rows_per_tap * kRowBytes, m, &c->full[s], p + dy * a.nx, z + dz, ci0, n);
+                tma_load4(sa + j * a.rows_per_tap * kWRowBytes, m, &c->full[s], p + dy * a.nx, z + dz, ci0, n);
             }
-            tma_load4(sa + kABytes, &mdy, &c->full[s], p, z, 0, n);
+            tma_load4(sa + a_bytes, &mdy, &c->full[s], p, z, 0, n);
             ++issued;
         }
-        if (aborted(c)) drain_loads<kStages>(c, issued);
+        if (aborted(c)) drain_loads<kWStages>(c, issued);
     } else if (threadIdx.x == 32) {
-        mma_loop<N, kStages, kABytes, 1, 0>(c, ring, tmem, ksteps);
+        mma_loop<N, kWStages, a_bytes, 1, 0, kWRowBytes>(c, ring, tmem, ksteps);
     }
     __syncwarp();
 
@@ -506,7 +530,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // bf16 tensor map of the given rank; dims innermost first, strides in bytes
 // for dims 1.., 64-byte swizzle, zero fill outside.
 int make_map(CUtensorMap *m, const void *base, int rank, const uint64_t *dims, const uint64_t *strides,
-             const uint32_t *box) {
+             const uint32_t *box, CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_64B) {
     auto fn = encode_fn();
     if (!fn) {
         set_error("cuTensorMapEncodeTiled is not available from the driver");
@@ -521,7 +545,7 @@ int make_map(CUtensorMap *m, const void *base, int rank, const uint64_t *dims, c
         if (i + 1 < rank) gs[i] = strides[i];
     }
     const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, rank, const_cast<void *>(base), gd, gs, bd, es,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         set_error("cuTensorMapEncodeTiled failed (" + std::to_string(static_cast<int>(r)) + ")");
@@ -539,13 +563,13 @@ int map_ndhwc(CUtensorMap *m, const void *p, int c, int nx, int ny, int nz, int 
     return make_map(m, p, 5, dims, st, box);
 }
 
-// channel-major activation [n][c][z][y*x]: box 32 voxels x rows channels
+// channel-major activation [n][c][z][y*x]: box 64 voxels x rows channels, 128-byte swizzle
 int map_ncdhw(CUtensorMap *m, const void *p, int c, int nxy, int nz, int nb, int rows) {
     const uint64_t dims[4] = {(uint64_t)nxy, (uint64_t)nz, (uint64_t)c, (uint64_t)nb};
     const uint64_t e = 2;
     const uint64_t st[3] = {(uint64_t)nxy * e, (uint64_t)nz * nxy * e, (uint64_t)c * nz * nxy * e};
-    const uint32_t box[4] = {32, 1, (uint32_t)rows, 1};
-    return make_map(m, p, 4, dims, st, box);
+    const uint32_t box[4] = {(uint32_t)kWK, 1, (uint32_t)rows, 1};
+    return make_map(m, p, 4, dims, st, box, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 // Dynamic shared memory of a ring (plus alignment slack and the control block).
@@ -553,6 +577,11 @@ int map_ncdhw(CUtensorMap *m, const void *p, int c, int nxy, int nz, int nb, int
 template <int N>
 size_t ring_smem() {
     return 1024 + kStages * (kABytes + N * kRowBytes) + sizeof(Ctrl);
+}
+
+template <int N>
+size_t wring_smem() {
+    return 1024 + kWStages * (kTileM * kWRowBytes + N * kWRowBytes) + sizeof(Ctrl);
 }
 
 template <int N>
@@ -578,7 +607,7 @@ int launch_fwd(const CUtensorMap &m1, const CUtensorMap &m2, const CUtensorMap &
 template <int N>
 int launch_wgrad(const CUtensorMap &mm, const CUtensorMap &m0, const CUtensorMap &mp, const CUtensorMap &md,
                  const WgradArgs &a, dim3 grid, cudaStream_t st) {
-    const size_t smem = ring_smem<N>();
+    const size_t smem = wring_smem<N>();
     static bool attr = false;
     if (!attr) {
         CT_CUDA(cudaFuncSetAttribute(conv_wgrad_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -686,8 +715,8 @@ int ct_unet_conv3d_wgrad(const void *xm, const void *x0, const void *xp, int cin
     CT_REQUIRE(ntaps == 1 || ntaps == 27, "conv3d_wgrad: ntaps must be 1 or 27");
     CT_REQUIRE(cin > 0 && cin % 32 == 0, "conv3d_wgrad: input channels must be a positive multiple of 32");
     CT_REQUIRE(valid_n(cout), "conv3d_wgrad: output channels must be 32, 64, 128 or 256");
-    CT_REQUIRE(nb > 0 && nz > 0 && ny > 0 && nx > 0 && nx % 8 == 0 && ((long long)nx * ny) % 32 == 0,
-               "conv3d_wgrad: x must be a multiple of 8 and x*y a multiple of 32");
+    CT_REQUIRE(nb > 0 && nz > 0 && ny > 0 && nx > 0 && nx % 8 == 0 && (long long)nx * ny < (1ll << 30),
+               "conv3d_wgrad: x must be a multiple of 8");
     CT_REQUIRE(kper > 0, "conv3d_wgrad: kper must be positive");
     CT_REQUIRE(aligned16(x0) && aligned16(dy) && (!xm || aligned16(xm)) && (!xp || aligned16(xp)),
                "conv3d_wgrad: pointers must be 16-byte aligned");
@@ -708,7 +737,9 @@ int ct_unet_conv3d_wgrad(const void *xm, const void *x0, const void *xp, int cin
     a.nxy = nxy;
     a.nx = nx;
     a.nz = nz;
-    a.kchunks = (long long)nb * nz * (nxy / 32);
+    // a slice past the end of a plane reads zeros for dY, so it adds nothing
+    a.pchunks = (nxy + kWK - 1) / kWK;
+    a.kchunks = (long long)nb * nz * a.pchunks;
     a.kper = kper;
     a.dw = dw;
     const int ttiles = (ntaps + a.taps_per_tile - 1) / a.taps_per_tile;

@@ -102,7 +102,7 @@ def conv3d_wgrad(xs, dy, ntaps=27, kper=None):
     cin = x0.shape[1]
     dw = torch.zeros((cout, ntaps, cin), dtype=torch.float32, device=dy.device)
     if kper is None:
-        chunks = n * z * y * x // 32
+        chunks = n * z * y * x // 64
         kper = max(16, -(-chunks // 1024))
     _lib.call("ct_unet_conv3d_wgrad", _p(xm), _tptr(x0), _p(xp), cin, _tptr(dyt), cout, n, z, y, x, ntaps, int(kper),
               _tptr(dw), _stream())

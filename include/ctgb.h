@@ -350,7 +350,8 @@ int ct_unet_conv3d(const void *d_x1, int c1, const void *d_x2, int c2, int nb, i
  * given channel-major [n][cin][z][y][x] as three copies shifted along x
  * (d_xm[x] = X[x - 1], d_x0, d_xp[x] = X[x + 1]; ct_unet_shift_t makes them;
  * d_xm / d_xp unused for ntaps 1); dY channel-major [n][cout][z][y][x].
- * Split-K: one CTA per kper 32-voxel slices. */
+ * x a multiple of 8.  Split-K: one CTA per kper 64-voxel slices of the y*x
+ * planes. */
 int ct_unet_conv3d_wgrad(const void *d_xm, const void *d_x0, const void *d_xp, int cin, const void *d_dy, int cout,
                          int nb, int nz, int ny, int nx, int ntaps, int kper, float *d_dw, void *stream);
 /* Reads and clears the device flag of the convolutions' bounded waits:

@@ -109,6 +109,8 @@ WGRAD_CASES = [
     ((32,), 64, 1, 1, 2, 16, 16, 4),
     ((128,), 32, 27, 1, 2, 2, 64, 1),
     ((32, 32), 64, 27, 1, 5, 16, 16, None),
+    ((64,), 128, 27, 2, 3, 4, 8, 1),                # y*x = 32: one slice runs past each plane
+    ((32,), 32, 27, 1, 2, 12, 8, 2),                # y*x = 96: the last slice is half outside
 ]
 
 

@@ -77,8 +77,11 @@ def test_asd_loop_graph_replays_eager_and_reduces_the_residual():
     assert torch.equal(again.x, graph.x)
     r = [v for _, v in eager.residuals]
     assert r[-1] < 0.5 * r[0]
-    stop = AsdLoop(plan, cfg).run(b, fdk, tol=r[10], check_every=1)
-    assert stop.iterations == 11 and ws.time_to_residual(stop, r[10])[0] == 11
+    # the residual norms are sums of FP64 atomics: equal between runs up to the last bits
+    tol = r[10] * (1 + 1e-6)
+    assert r[9] > tol
+    stop = AsdLoop(plan, cfg).run(b, fdk, tol=tol, check_every=1)
+    assert stop.iterations == 11 and ws.time_to_residual(stop, tol)[0] == 11
 
 
 @pytest.mark.gpu
