@@ -63,3 +63,40 @@ def test_argument_validation_needs_no_gpu():
                                  beta.ctypes.data_as(C.c_void_p), 4, P.ctypes.data_as(C.c_void_p), 8,
                                  P.ctypes.data_as(C.c_void_p), 8, 100.0)
     assert st == 1
+
+
+def test_unet_and_asd_argument_validation_needs_no_gpu():
+    """The warm-start kernels' entry points reject bad shapes, channel counts
+    and pointers before any CUDA call (the pointers here are never dereferenced)."""
+    import ctypes as C
+    from ctgb import _lib
+    lib = _lib.load()
+    p, q = C.c_void_p(0x10000), C.c_void_p(0x20000)        # 16-byte aligned, never used
+    odd = C.c_void_p(0x10004)
+
+    def conv(c1=32, c2=0, nz=4, ny=16, nx=16, taps=27, co1=32, co2=0, x1=p, out1=q):
+        return lib.ct_unet_conv3d(x1, c1, p if c2 else None, c2, 1, nz, ny, nx, p, taps, None, 1, out1, co1,
+                                  q if co2 else None, co2, None, None, None)
+
+    assert conv(c1=16) == 1 and b"multiples of 32" in lib.ct_last_error()
+    assert conv(co1=32, co2=16) == 1 and b"256" in lib.ct_last_error()
+    assert conv(taps=9) == 1
+    assert conv(nx=12) == 1 and b"128" in lib.ct_last_error()
+    assert conv(x1=odd) == 1 and b"aligned" in lib.ct_last_error()
+    assert conv(out1=None) == 1
+
+    def wgrad(cin=32, cout=32, nx=16, ny=16, kper=4, taps=27):
+        return lib.ct_unet_conv3d_wgrad(p, p, p, cin, q, cout, 1, 4, ny, nx, taps, kper, q, None)
+
+    assert wgrad(cin=48) == 1
+    assert wgrad(cout=96) == 1
+    assert wgrad(nx=12) == 1 and b"multiple of 8" in lib.ct_last_error()
+    assert wgrad(kper=0) == 1
+    assert lib.ct_unet_pool2(p, q, 12, 1, 2, 2, 2, None) == 1
+    assert lib.ct_unet_up2(p, None, 32, 1, 2, 2, 2, None) == 1
+    assert lib.ct_unet_shift_t(p, 32, 1, 2, 2, 8, None, q, None, 48, 32, None) == 1
+    assert lib.ct_unet_colsum(p, 48, 100, q, None) == 1
+    assert lib.ct_unet_head(p, None, p, None, q, 100, None) == 1
+    assert lib.ct_unet_im2col27(p, 1, 0, 4, 4, q, None) == 1
+    assert lib.ct_tv_flow_asd(p, None, p, p, p, 4, 4, 4, 2, 1e-8, 0.0, 0.95, 0.95, None) == 1
+    assert lib.ct_tv_flow_asd(p, p, p, p, p, 4, 4, 4, -1, 1e-8, 0.0, 0.95, 0.95, None) == 1
