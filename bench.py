@@ -331,7 +331,8 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (512 MiB volume, 566 MB sinogram, 2.3 GB packed quads)",
                        "phantom": "12 random ellipsoids, seed 2"},
             "roofline": roofline, "kernels": kern, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": 3 * args.steps, "sirt_tv_learned_vs_plain": warm}
+            # per step: transpose_ts, cone_fp, cone_fixup, pack_quads, cone_bp (the ncu launch list)
+            "gpu_launches": 5 * args.steps, "sirt_tv_learned_vs_plain": warm}
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
