@@ -30,7 +30,6 @@ import ctypes as C
 import math
 from dataclasses import dataclass, field
 
-import numpy as np
 import torch
 
 from . import _lib
@@ -55,7 +54,8 @@ def _p(t):
 
 
 def status() -> int:
-    """Raise if a convolution's bounded wait gave up since the last check."""
+    """0 when no bounded wait of the convolutions gave up since the last call;
+    otherwise raises CTError (CT_ERR_TIMEOUT).  Clears the device flag."""
     flags = C.c_int(0)
     _lib.call("ct_unet_status", C.byref(flags))
     return flags.value
@@ -176,6 +176,9 @@ LAYERS = [
 ]
 
 
+_RELU = {name: relu for name, _, _, _, relu in LAYERS}
+
+
 def flops_per_voxel() -> float:
     """Multiply-adds x 2 of one forward pass per full-resolution voxel."""
     level = {"e1": 1, "d1": 1, "u1": 8, "e2": 8, "d2": 8, "u2": 64, "e3": 64, "d3": 64, "u3": 512, "b": 512}
@@ -238,8 +241,7 @@ class UNet3D:
 
     # forward -------------------------------------------------------------------
     def _conv(self, name, *xs, ntaps):
-        spec = {n: (ci, co, t, r) for n, ci, co, t, r in LAYERS}[name]
-        return conv3d(xs[0], self.wb[name], self.params[name + ".b"], relu=spec[3],
+        return conv3d(xs[0], self.wb[name], self.params[name + ".b"], relu=_RELU[name],
                       x2=xs[1] if len(xs) > 1 else None, ntaps=ntaps)
 
     def forward(self, x: torch.Tensor, keep: bool = False):
