@@ -494,7 +494,7 @@ conv_wgrad_kernel(const __grid_constant__ CUtensorMap mxm, const __grid_constant
     const int tap = tap0 + r / a.rows_per_tap, ci = ci0 + r % a.rows_per_tap;
     const bool valid = ok && ksteps > 0 && tap < a.ntaps;
     const uint32_t trow = tmem + (static_cast<uint32_t>(warp * 32) << 16);
-    float *dst = a.dw + static_cast<long long>(tap) * a.cin + ci;
+    float *dst = a.dw + (valid ? static_cast<long long>(tap) * a.cin + ci : 0);   // rows past the last tap: unused
     const long long cstride = static_cast<long long>(a.ntaps) * a.cin;
 #pragma unroll 1
     for (int c0 = 0; c0 < N; c0 += 16) {
