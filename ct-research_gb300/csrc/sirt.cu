@@ -39,7 +39,9 @@ tv_grad_kernel(const float *__restrict__ x, float *__restrict__ g, int nx, int n
     const int j = blockIdx.y * TV_BY + threadIdx.y;
     double s = 0.0;
     // each thread walks z with the grid's z stride, so one launch adds a few
-    // thousand block sums to *sumsq instead of one per 256 voxels
+    // thousand block sums to *sumsq instead of one per 256 voxels; unrolled so
+    // that several planes' loads are in flight per thread
+#pragma unroll 4
     for (int k = blockIdx.z * TV_BZ + threadIdx.z; i < nx && j < ny && k < nz; k += gridDim.z * TV_BZ) {
         float dx, dy, dz, in;
         fdiff(x, nx, ny, nz, i, j, k, eps2, dx, dy, dz, in);
