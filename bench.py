@@ -573,6 +573,44 @@ def run_unet(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sirt_step(args):
+    """The parts of one SIRT-TV iteration of the warm-start comparison (512^3, 90
+    views, ASD step), each timed with CUDA events after 3 warm-up iterations:
+    FP + residual, BP + update, and the 20 TV sub-steps."""
+    import torch
+    import ctgb
+    from ctgb import device as dev, warmstart as ws
+    from ctgb.device import ConePlan
+    from ctgb.sirt import AsdConfig, AsdLoop
+    ctgb.load()
+    plan = ConePlan(ws.scan(512, 90))
+    vol = ws.phantom_volume(512, 7)
+    b = plan.fp(vol)
+    loop = AsdLoop(plan, AsdConfig(iters=3))
+    loop.run(b, plan.fdk(b), iters=3)
+    s, x = loop.s, loop.x
+    parts = {"fp_residual": [], "bp_update": [], "tv_20_substeps": []}
+    for _ in range(max(1, args.steps)):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        loop.prev.copy_(x)
+        s.norms.zero_()
+        ev[0].record()
+        plan.fp_residual(x, loop.b, s.rowsum, 1e-9, out=s.e, norms=s.norms)
+        ev[1].record()
+        plan.bp_update(s.e, s.colsum, x, lam=1.0, eps=1e-9, lo=0.0, hi=float("inf"))
+        ev[2].record()
+        dev.tv_flow_asd(x, loop.prev, loop.work, loop.scratch, loop.state, 20, 1e-8, 0.0, 0.95, 0.95)
+        ev[3].record()
+        torch.cuda.synchronize()
+        for k, (a, c) in zip(parts, ((0, 1), (1, 2), (2, 3))):
+            parts[k].append(ev[a].elapsed_time(ev[c]))
+    med = {k: float(np.median(v)) for k, v in parts.items()}
+    line = {"metric": "SIRT-TV iteration parts at 512^3 / 90 views", "unit": "ms", "value": sum(med.values()),
+            "higher_is_better": False, "parts_ms": med, "steps": args.steps,
+            "config": {"workload": "cone_512 geometry with 90 views, ASD-POCS TV step, 20 sub-steps"}}
+    print(json.dumps(line), flush=True)
+
+
 def run_fdk(args):
     """FDK of the 256^3 / 360-view / 512x384 cone scan (reference launch-order
     filter and sticky backprojection)."""
@@ -732,7 +770,7 @@ def main():
                     help="small: the profiling case of the same kernels (pair: 256^3 / 90 views / 384x256; "
                          "unet: 128^3 layers and network)")
     ap.add_argument("--workload", choices=["pair", "batched2d", "sirt_tv", "fdk", "fan2d", "iterfdk", "fdkui",
-                                           "warmstart", "unet"], default="pair",
+                                           "warmstart", "unet", "sirt_step"], default="pair",
                     help="pair (default): the FP+BP throughput line; the others report their own metric")
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     ap.add_argument("--ref-iters", type=int, default=500, help="reference SIRT-TV iterations (--workload warmstart)")
@@ -747,7 +785,7 @@ def main():
     else:
         {"batched2d": run_batched2d, "sirt_tv": run_sirt_tv, "fdk": run_fdk, "fan2d": run_fan2d,
          "iterfdk": run_iterfdk, "fdkui": run_fdkui, "warmstart": run_warmstart,
-         "unet": run_unet}[args.workload](args)
+         "unet": run_unet, "sirt_step": run_sirt_step}[args.workload](args)
 
 
 if __name__ == "__main__":
