@@ -41,7 +41,7 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
     const bool active = p < g.np && x < g.nx;
     const int nmax = g.nt * g.ns * g.nz - 1;
     const long long o = ((long long)v * g.nx + x) * g.np + p;
-    double r2 = 0.0, b2 = 0.0;
+    float r2 = 0.0f, b2 = 0.0f;    // per-ray terms of the norms (FP32; block sums in FP64)
     if (active) {
         RayWalk w;
         // detector neighbours in P are offset along (cos b, sin b): read the copy
@@ -51,7 +51,7 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
         const bool use_t = volT && fabs(tr.x) > fabs(tr.y);
         const bool hit = ray_setup(g, v, p, x, use_t, w);
         if (MODE == 2) {
-            r2 = hit ? (double)w.nseg : 0.0;
+            r2 = hit ? (float)w.nseg : 0.0f;   // exact: counts < 2^19
         } else {
             if (hit && w.grazing) {
                 const int slot = atomicAdd(gl.count, 1);
@@ -65,16 +65,16 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
                 const float r = bb - val;
                 const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
                 out[o] = r * sc;
-                r2 = (hit && w.grazing) ? 0.0 : (double)r * r;   // grazing rays: added by the FP64 re-walk
-                b2 = (double)bb * bb;
+                r2 = (hit && w.grazing) ? 0.0f : r * r;   // grazing rays: added by the FP64 re-walk
+                b2 = bb * bb;
             }
         }
     }
     if (MODE == 1) {
-        block_sum_atomic<FP_BX * FP_BY / 32>(r2, norms);
-        block_sum_atomic<FP_BX * FP_BY / 32>(b2, norms + 1);
+        block_sum_atomic_f<FP_BX * FP_BY / 32>(r2, norms);
+        block_sum_atomic_f<FP_BX * FP_BY / 32>(b2, norms + 1);
     } else if (MODE == 2) {
-        block_sum_atomic<FP_BX * FP_BY / 32>(r2, norms);
+        block_sum_atomic_f<FP_BX * FP_BY / 32>(r2, norms);
     }
 }
 

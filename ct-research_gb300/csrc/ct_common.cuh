@@ -79,4 +79,24 @@ __device__ __forceinline__ void block_sum_atomic(double v, double *out) {
     }
 }
 
+// The same for per-thread FP32 terms: the warp sums (32 terms) run in FP32,
+// the per-warp partials and the atomic in FP64.  GB300 runs FP64 at a small
+// fraction of its FP32 rate, so a per-element FP64 reduction can bound an
+// otherwise memory-bound kernel; these sums normalise steps and report
+// residuals, for which FP32 partials of 32 terms are ample.  Integer-valued
+// terms below 2^19 sum exactly.
+template <int NWARPS>
+__device__ __forceinline__ void block_sum_atomic_f(float v, double *out) {
+    __shared__ double part[NWARPS];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    v = warp_sum(v);
+    if ((tid & 31) == 0) part[tid >> 5] = (double)v;
+    __syncthreads();
+    if (tid < 32) {
+        double w = (tid < NWARPS) ? part[tid] : 0.0;
+        w = warp_sum(w);
+        if (tid == 0) atomicAdd(out, w);
+    }
+}
+
 }  // namespace ct

@@ -17,7 +17,7 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
               double *__restrict__ norms, const GrazeList gl) {
     const long long r = (long long)blockIdx.x * F2_BLOCK + threadIdx.x;
     const bool active = r < (long long)g.nb * g.np;
-    double r2 = 0.0, b2 = 0.0;
+    float r2 = 0.0f, b2 = 0.0f;
     if (active) {
         bool grazing;
         const float val = fan_ray_value(g, img, r, grazing);
@@ -32,13 +32,13 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
             const float rr = bb - val;
             const float sc = rowsum ? 1.0f / (rowsum[r] + eps) : 1.0f;
             out[r] = (OutT)(rr * sc);
-            r2 = grazing ? 0.0 : (double)rr * rr;   // grazing rays: added by the FP64 re-walk
-            b2 = (double)bb * bb;
+            r2 = grazing ? 0.0f : rr * rr;   // grazing rays: added by the FP64 re-walk
+            b2 = bb * bb;
         }
     }
     if (MODE == 1) {
-        block_sum_atomic<F2_BLOCK / 32>(r2, norms);
-        block_sum_atomic<F2_BLOCK / 32>(b2, norms + 1);
+        block_sum_atomic_f<F2_BLOCK / 32>(r2, norms);
+        block_sum_atomic_f<F2_BLOCK / 32>(b2, norms + 1);
     }
 }
 

@@ -142,4 +142,19 @@ __device__ __forceinline__ void block_sum_any(double v, double *out) {
     __syncthreads();
 }
 
+// block_sum_any for per-thread FP32 terms (FP32 warp sums, FP64 partials).
+__device__ __forceinline__ void block_sum_any_f(float v, double *out) {
+    __shared__ double part[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0) part[wid] = (double)v;
+    __syncthreads();
+    if (wid == 0) {
+        double w = lane < nw ? part[lane] : 0.0;
+        w = warp_sum(w);
+        if (lane == 0) atomicAdd(out, w);
+    }
+    __syncthreads();
+}
+
 }  // namespace ct

@@ -42,7 +42,7 @@ fan_batch_fp_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__r
     const FanGeom g = sl[k].g;
     const long long r = (long long)(blockIdx.x - sl[k].ray_blk0) * blockDim.x + threadIdx.x;
     const bool active = r < (long long)g.nb * g.np;
-    double r2 = 0.0, b2 = 0.0;
+    float r2 = 0.0f, b2 = 0.0f;
     if (active) {
         bool grazing;
         const float val = fan_ray_value(g, img + sl[k].img_off, r, grazing);
@@ -58,13 +58,13 @@ fan_batch_fp_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__r
             const float rr = bb - val;
             const float sc = rowsum ? 1.0f / (rowsum[o] + eps) : 1.0f;
             out[o] = rr * sc;
-            r2 = grazing ? 0.0 : (double)rr * rr;   // grazing rays: added by the FP64 re-walk
-            b2 = (double)bb * bb;
+            r2 = grazing ? 0.0f : rr * rr;   // grazing rays: added by the FP64 re-walk
+            b2 = bb * bb;
         }
     }
     if (MODE == 1) {
-        block_sum_any(r2, norms + 2 * k);
-        block_sum_any(b2, norms + 2 * k + 1);
+        block_sum_any_f(r2, norms + 2 * k);
+        block_sum_any_f(b2, norms + 2 * k + 1);
     }
 }
 

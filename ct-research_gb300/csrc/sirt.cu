@@ -16,7 +16,7 @@ namespace ct {
 
 namespace {
 
-constexpr int TV_BX = 32, TV_BY = 4, TV_BZ = 2;
+constexpr int TV_BX = 32, TV_BY = 8;   // gradient block: 32 x 8 columns
 
 __device__ __forceinline__ float ld(const float *__restrict__ x, int i) { return __ldg(x + i); }
 
@@ -32,39 +32,108 @@ __device__ __forceinline__ void fdiff(const float *__restrict__ x, int nx, int n
     inv_n = rsqrtf(dx * dx + dy * dy + dz * dz + eps2);
 }
 
-__global__ void __launch_bounds__(TV_BX * TV_BY * TV_BZ)
-tv_grad_kernel(const float *__restrict__ x, float *__restrict__ g, int nx, int ny, int nz, float eps2,
+// The gradient of one sub-step.  A block owns a 32 x 8 tile of columns and a
+// run of kc planes; it keeps three planes of x (the tile plus a one-voxel halo
+// on every side, 34 x 10) in shared memory, prefetching the plane after next
+// into registers while it works on the current one.  Each voxel's forward
+// differences and norm are evaluated once (as fdiff does, same operations)
+// and shared through shared memory with the voxels whose backward terms need
+// them; threads 0-39 also evaluate the 40 halo points (column i0 - 1, row
+// j0 - 1) whose terms the tile's edge voxels need; the (i, j, k-1) term stays
+// in a register from the previous plane.  One double atomic per block.
+__global__ void __launch_bounds__(TV_BX * TV_BY)
+tv_grad_kernel(const float *__restrict__ x, float *__restrict__ g, int nx, int ny, int nz, int kc, float eps2,
                double *__restrict__ sumsq) {
-    const int i = blockIdx.x * TV_BX + threadIdx.x;
-    const int j = blockIdx.y * TV_BY + threadIdx.y;
-    double s = 0.0;
-    // each thread walks z with the grid's z stride, so one launch adds a few
-    // thousand block sums to *sumsq instead of one per 256 voxels; unrolled so
-    // that several planes' loads are in flight per thread
-#pragma unroll 4
-    for (int k = blockIdx.z * TV_BZ + threadIdx.z; i < nx && j < ny && k < nz; k += gridDim.z * TV_BZ) {
-        float dx, dy, dz, in;
-        fdiff(x, nx, ny, nz, i, j, k, eps2, dx, dy, dz, in);
-        float gv = -(dx + dy + dz) * in;
-        if (i > 0) {
-            float ax, ay, az, an;
-            fdiff(x, nx, ny, nz, i - 1, j, k, eps2, ax, ay, az, an);
-            gv += ax * an;
-        }
-        if (j > 0) {
-            float ax, ay, az, an;
-            fdiff(x, nx, ny, nz, i, j - 1, k, eps2, ax, ay, az, an);
-            gv += ay * an;
-        }
-        if (k > 0) {
-            float ax, ay, az, an;
-            fdiff(x, nx, ny, nz, i, j, k - 1, eps2, ax, ay, az, an);
-            gv += az * an;
-        }
-        g[(k * ny + j) * nx + i] = gv;
-        s += (double)gv * gv;
+    constexpr int W = TV_BX + 2, H = TV_BY + 2, NT = TV_BX * TV_BY, PW = W * H;
+    static_assert(PW <= 2 * NT && TV_BX + TV_BY <= NT, "tile and halo sizes");
+    __shared__ float T[3 * PW];
+    __shared__ float Px[H][W], Py[H][W];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TV_BX + tx;
+    const int i0 = blockIdx.x * TV_BX, j0 = blockIdx.y * TV_BY;
+    const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
+    const int plane = nx * ny;
+    const int i = i0 + tx, j = j0 + ty;
+    const bool in = i < nx && j < ny;
+    // tile element e -> clamped global offset in a plane (halo outside the volume: never used)
+    auto toff = [&](int e) {
+        const int gi = min(max(i0 - 1 + e % W, 0), nx - 1), gj = min(max(j0 - 1 + e / W, 0), ny - 1);
+        return gj * nx + gi;
+    };
+    const int e1 = tid + NT;
+    const bool has1 = e1 < PW;
+    const int o0 = toff(tid), o1 = has1 ? toff(e1) : 0;
+    // halo point of this thread (tid < 40): column i0 - 1 for tid < 8, row j0 - 1 for 8 <= tid < 40
+    const bool hcol = tid < TV_BY, hrow = tid >= TV_BY && tid < TV_BY + TV_BX;
+    const int hr = hcol ? tid + 1 : 0, hc = hcol ? 0 : tid - TV_BY + 1;          // tile coordinates
+    const int hgi = i0 - 1 + hc, hgj = j0 - 1 + hr;                                // global coordinates
+    const bool hdo = (hcol && i0 > 0 && hgj < ny) || (hrow && j0 > 0 && hgi < nx);
+    // plane buffers, rotated each plane: cur (k), nxt (k + 1), spare (k - 1, then k + 2)
+    int cur = 0, nxt = PW, spare = 2 * PW;
+    const int zk1 = min(k0 + 1, nz - 1);
+    T[cur + tid] = __ldg(x + k0 * plane + o0);
+    T[nxt + tid] = __ldg(x + zk1 * plane + o0);
+    if (has1) {
+        T[cur + e1] = __ldg(x + k0 * plane + o1);
+        T[nxt + e1] = __ldg(x + zk1 * plane + o1);
     }
-    block_sum_atomic<TV_BX * TV_BY * TV_BZ / 32>(s, sumsq);
+    float pz_prev = 0.0f;
+    if (in && k0 > 0) {
+        float ax, ay, az, an;
+        fdiff(x, nx, ny, nz, i, j, k0 - 1, eps2, ax, ay, az, an);
+        pz_prev = az * an;
+    }
+    __syncthreads();
+    float s = 0.0f;                 // this thread's g^2 over its (at most 32) planes
+    const float *px0 = x + o0, *px1 = x + o1;
+    for (int k = k0; k < k1; ++k) {
+        const bool more = k + 1 < k1;                        // the next plane needs plane k + 2
+        float r0 = 0.0f, r1 = 0.0f;
+        if (more) {
+            const int zp = min(k + 2, nz - 1) * plane;
+            r0 = __ldg(px0 + zp);
+            if (has1) r1 = __ldg(px1 + zp);
+        }
+        const bool zf = k + 1 < nz;
+        // forward differences and norm at tile point (r, c) = global (gi, gj, k), as fdiff
+        auto fd = [&](int r, int c, int gi, int gj, float &dx, float &dy, float &dz, float &inv_n) {
+            const int e = r * W + c;
+            const float v = T[cur + e];
+            dx = (gi + 1 < nx) ? T[cur + e + 1] - v : 0.0f;
+            dy = (gj + 1 < ny) ? T[cur + e + W] - v : 0.0f;
+            dz = zf ? T[nxt + e] - v : 0.0f;
+            inv_n = rsqrtf(dx * dx + dy * dy + dz * dz + eps2);
+        };
+        float dx, dy, dz, inv_n;
+        fd(ty + 1, tx + 1, i, j, dx, dy, dz, inv_n);
+        Px[ty + 1][tx + 1] = dx * inv_n;
+        Py[ty + 1][tx + 1] = dy * inv_n;
+        if (hdo) {
+            float ax, ay, az, an;
+            fd(hr, hc, hgi, hgj, ax, ay, az, an);
+            if (hcol) Px[hr][0] = ax * an;
+            else Py[0][hc] = ay * an;
+        }
+        __syncthreads();
+        float gv = -(dx + dy + dz) * inv_n;
+        if (i > 0) gv += Px[ty + 1][tx];
+        if (j > 0) gv += Py[ty][tx + 1];
+        if (k > 0) gv += pz_prev;
+        pz_prev = dz * inv_n;
+        if (in) {
+            g[k * plane + j * nx + i] = gv;
+            s = fmaf(gv, gv, s);
+        }
+        if (more) {                                          // plane k + 2 replaces plane k - 1
+            T[spare + tid] = r0;
+            if (has1) T[spare + e1] = r1;
+        }
+        const int t = cur;
+        cur = nxt;
+        nxt = spare;
+        spare = t;
+        __syncthreads();
+    }
+    block_sum_atomic_f<TV_BX * TV_BY / 32>(s, sumsq);
 }
 
 __global__ void __launch_bounds__(256)
@@ -73,6 +142,7 @@ tv_apply_kernel(float *__restrict__ x, const float *__restrict__ g, long long n,
     const double ss = *sumsq;
     if (!(ss > 0.0)) return;
     const float scale = (float)(step * sqrt((double)n / ss));
+#pragma unroll 4
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         x[i] = fmaxf(fmaf(-scale, g[i], x[i]), lo);
 }
@@ -86,6 +156,7 @@ tv_apply_asd_kernel(float *__restrict__ x, const float *__restrict__ g, long lon
     const double ss = *sumsq, dp2 = state[1];
     if (!(ss > 0.0) || !(dp2 > 0.0)) return;
     const float scale = (float)(state[0] * sqrt(dp2 / ss));
+#pragma unroll 4
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         x[i] = fmaxf(fmaf(-scale, g[i], x[i]), lo);
 }
@@ -97,20 +168,31 @@ __global__ void asd_alpha_kernel(double *state, float alpha_red, float r_max) {
 
 __global__ void __launch_bounds__(256)
 sq_diff_kernel(const float *__restrict__ a, const float *__restrict__ b, long long n, double *__restrict__ out) {
+    // FP32 partial sums of 16 terms, flushed into an FP64 sum (FP64 per
+    // element would bound this kernel on GB300)
     double s = 0.0;
+    float f = 0.0f;
+    int c = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float d = a[i] - b[i];
-        s += (double)d * d;
+        f = fmaf(d, d, f);
+        if (++c == 16) {
+            s += (double)f;
+            f = 0.0f;
+            c = 0;
+        }
     }
+    s += (double)f;
     block_sum_atomic<8>(s, out);
 }
 
-// xy tiles of the volume, and z blocks up to ~16 blocks per SM in total
-dim3 tv_grid(int nx, int ny, int nz) {
-    const int gx = (nx + TV_BX - 1) / TV_BX, gy = (ny + TV_BY - 1) / TV_BY, zb = (nz + TV_BZ - 1) / TV_BZ;
-    const long long want = 16LL * sm_count();
-    const int gz = (int)std::max<long long>(1, std::min<long long>(zb, want / ((long long)gx * gy)));
-    return dim3(gx, gy, gz);
+// 32 x 8 column tiles, and runs of kc planes: up to 32, fewer when that leaves
+// under ~8 blocks per SM
+dim3 tv_grid(int nx, int ny, int nz, int &kc) {
+    const long long gx = (nx + TV_BX - 1) / TV_BX, gy = (ny + TV_BY - 1) / TV_BY;
+    const long long fill = gx * gy * nz / (8LL * sm_count());
+    kc = (int)std::min<long long>(nz, std::max<long long>(2, std::min<long long>(32, fill)));
+    return dim3((unsigned)gx, (unsigned)gy, (unsigned)((nz + kc - 1) / kc));
 }
 
 }  // namespace
@@ -120,12 +202,13 @@ int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int n
     CT_REQUIRE(nx > 0 && ny > 0 && nz > 0, "tv: sizes must be positive");
     CT_REQUIRE((long long)nx * ny * nz < (1LL << 31), "tv: volume too large");
     const long long n = (long long)nx * ny * nz;
-    dim3 block(TV_BX, TV_BY, TV_BZ);
-    const dim3 grid = tv_grid(nx, ny, nz);
+    dim3 block(TV_BX, TV_BY);
+    int kc = 1;
+    const dim3 grid = tv_grid(nx, ny, nz, kc);
     const int ablocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     for (int it = 0; it < iters; ++it) {
         CT_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double), st), "tv memset");
-        tv_grad_kernel<<<grid, block, 0, st>>>(x, work, nx, ny, nz, eps * eps, scratch);
+        tv_grad_kernel<<<grid, block, 0, st>>>(x, work, nx, ny, nz, kc, eps * eps, scratch);
         CT_LAUNCH_CHECK("tv_grad_kernel");
         tv_apply_kernel<<<ablocks, 256, 0, st>>>(x, work, n, step, lo, scratch);
         CT_LAUNCH_CHECK("tv_apply_kernel");
@@ -138,15 +221,16 @@ int tv_flow_asd_launch(float *x, float *prev, float *work, double *scratch, doub
     CT_REQUIRE(nx > 0 && ny > 0 && nz > 0, "tv: sizes must be positive");
     CT_REQUIRE((long long)nx * ny * nz < (1LL << 31), "tv: volume too large");
     const long long n = (long long)nx * ny * nz;
-    dim3 block(TV_BX, TV_BY, TV_BZ);
-    const dim3 grid = tv_grid(nx, ny, nz);
+    dim3 block(TV_BX, TV_BY);
+    int kc = 1;
+    const dim3 grid = tv_grid(nx, ny, nz, kc);
     const int ablocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 8);
     CT_CUDA(cudaMemsetAsync(state + 1, 0, 2 * sizeof(double), st), "asd memset");
     if (int s = sq_diff_sum_launch(x, prev, n, state + 1, st)) return s;        // dp2
     CT_CUDA(cudaMemcpyAsync(prev, x, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "asd copy");
     for (int it = 0; it < iters; ++it) {
         CT_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double), st), "tv memset");
-        tv_grad_kernel<<<grid, block, 0, st>>>(x, work, nx, ny, nz, eps * eps, scratch);
+        tv_grad_kernel<<<grid, block, 0, st>>>(x, work, nx, ny, nz, kc, eps * eps, scratch);
         CT_LAUNCH_CHECK("tv_grad_kernel");
         tv_apply_asd_kernel<<<ablocks, 256, 0, st>>>(x, work, n, lo, scratch, state);
         CT_LAUNCH_CHECK("tv_apply_asd_kernel");

@@ -324,7 +324,8 @@ int ct_tv_flow(float *d_x, float *d_work, double *d_scratch, int nx, int ny, int
  * alpha_red when the sub-steps moved x by more than r_max * dp. */
 int ct_tv_flow_asd(float *d_x, float *d_prev, float *d_work, double *d_scratch, double *d_state, int nx, int ny,
                    int nz, int iters, float eps, float lo, float alpha_red, float r_max, void *stream);
-/* d_norm[0] += sum((a - b)^2) over n floats (double accumulation). */
+/* d_norm[0] += sum((a - b)^2) over n floats (FP32 partial sums of 16 terms,
+ * accumulated in double). */
 int ct_sq_diff_sum(const float *d_a, const float *d_b, long long n, double *d_norm, void *stream);
 
 /* ===================================================================== */

@@ -265,7 +265,8 @@ def test_fp_residual_fused_matches_unfused(torch_cuda):
     assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) <= 1e-6
     r = (b - plan.fp(x)).double()
     assert abs(norms[0].item() - (r * r).sum().item()) <= 1e-6 * (r * r).sum().item()
-    assert abs(norms[1].item() - (b.double() ** 2).sum().item()) <= 1e-9 * (b.double() ** 2).sum().item()
+    # the norms sum FP32 squares in FP32 warp partials (32 terms), then in FP64
+    assert abs(norms[1].item() - (b.double() ** 2).sum().item()) <= 1e-6 * (b.double() ** 2).sum().item()
 
 
 def test_bp_update_fused_matches_unfused(torch_cuda):
