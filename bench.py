@@ -419,9 +419,9 @@ def run_sirt_tv(args):
 def run_warmstart(args):
     seeds = [int(v) for v in args.seeds.split(",")]
     if len(seeds) == 1:
-        print(json.dumps(measure_warmstart(args.ref_iters, seeds[0])), flush=True)
+        print(json.dumps(measure_warmstart(args.ref_iters, seeds[0], args.weights)), flush=True)
         return
-    runs = [measure_warmstart(args.ref_iters, sd) for sd in seeds]
+    runs = [measure_warmstart(args.ref_iters, sd, args.weights) for sd in seeds]
     sp = [r["speedup"] for r in runs if r["speedup"] is not None]
     line = {"metric": "SIRT-TV wall time to the 500-iteration data residual, learned start", "unit": "s",
             "value": float(np.mean([r["value"] for r in runs if r["value"] is not None])), "higher_is_better": False,
@@ -438,7 +438,7 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_warmstart(ref_iters: int = 500, seed: int = 7) -> dict:
+def measure_warmstart(ref_iters: int = 500, seed: int = 7, weights: str | None = None) -> dict:
     """Learned warm start vs plain SIRT-TV on the sparse-view 512^3 scan (90 views
     over 360 deg, the cone_512 detector and distances), noise-free data of a
     12-ellipsoid phantom (seed 7 unless given; training used seeds 1000-2999).
@@ -461,7 +461,8 @@ def measure_warmstart(ref_iters: int = 500, seed: int = 7) -> dict:
     vol = ws.phantom_volume(n, seed)
     b = plan.fp(vol)
     fdk = plan.fdk(b)
-    net = ws.load()
+    wpath = Path(weights).resolve() if weights else ws.WEIGHTS
+    net = ws.load(wpath)
     loop = AsdLoop(plan, AsdConfig(iters=iters))
     ref = loop.run(b, fdk, check_every=1)
     tol = ref.residuals[-1][1]
@@ -508,7 +509,7 @@ def measure_warmstart(ref_iters: int = 500, seed: int = 7) -> dict:
             "dtype": "bf16 network / f32 SIRT-TV", "data": "synthetic (seeded ellipsoid phantoms, noise-free)",
             "config": {"workload": "cone_512 geometry with 90 views; U-Net trained on 128^3 pairs of the same scan "
                                    "(90-view FDK -> 500-iteration SIRT-TV)",
-                       "weights": str(ws.WEIGHTS.relative_to(ROOT))}}
+                       "weights": str(wpath.relative_to(ROOT)) if wpath.is_relative_to(ROOT) else str(wpath)}}
     return line
 
 
@@ -775,6 +776,8 @@ def main():
     ap.add_argument("--iters", type=int, default=200, help="SIRT-TV iterations (--workload sirt_tv)")
     ap.add_argument("--ref-iters", type=int, default=500, help="reference SIRT-TV iterations (--workload warmstart)")
     ap.add_argument("--seeds", default="7", help="phantom seeds, comma-separated (--workload warmstart)")
+    ap.add_argument("--weights", default=None, help="U-Net weights (.npz) for --workload warmstart; default: the "
+                                                     "committed ones")
     args = ap.parse_args()
     if args.warmup < 3:
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

@@ -179,6 +179,8 @@ def _main(argv=None):
     ap.add_argument("--seed0", type=int, default=1000)
     ap.add_argument("--holdout", type=int, default=4)
     ap.add_argument("--out", type=Path, default=WEIGHTS)
+    ap.add_argument("--init", type=Path, default=None, help="start from these weights (fine-tuning)")
+    ap.add_argument("--lr-end", type=float, default=3e-5)
     args = ap.parse_args(argv)
 
     def log(m):
@@ -190,15 +192,17 @@ def _main(argv=None):
     pairs = generate(args.pairs, args.n, args.views, args.iters, args.seed0, log=log)
     log(f"generated {args.pairs} pairs in {pairs.seconds:.1f} s; target residual median "
         f"{float(np.median(pairs.residuals)):.3e}")
-    net = unet.UNet3D(seed=0)
+    net = load(args.init) if args.init else unet.UNet3D(seed=0)
     meta = dict(pairs=args.pairs, n=args.n, views=args.views, iters=args.iters, seed0=args.seed0,
-                gen_seconds=round(pairs.seconds, 1))
+                gen_seconds=round(pairs.seconds, 1), lr=args.lr, lr_end=args.lr_end)
+    if args.init:
+        meta["init"] = str(np.load(args.init)["meta"])
 
     def on_epoch(ep, hist):
         save(net, args.out, **meta, epochs_done=ep + 1, loss=[round(v, 8) for v in hist])
 
     tt = time.perf_counter()
-    hist = train(net, pairs, epochs=args.epochs, lr=args.lr, log=log, on_epoch=on_epoch)
+    hist = train(net, pairs, epochs=args.epochs, lr=args.lr, lr_end=args.lr_end, log=log, on_epoch=on_epoch)
     meta["train_seconds"] = round(time.perf_counter() - tt, 1)
     del pairs
     torch.cuda.empty_cache()
