@@ -91,3 +91,18 @@ def test_untrained_network_start_is_the_fdk_volume():
     fdk = torch.rand((128, 128, 128), device="cuda")
     assert torch.equal(ws.warm_start(net, fdk), fdk)
     assert rel_l2(ws.warm_start(net, fdk, train_n=64).cpu().numpy(), fdk.cpu().numpy()) <= 1e-6
+
+
+def test_weights_round_trip_through_save_and_load(tmp_path):
+    """save() stores bf16 weights with their metadata; load() (also used to
+    fine-tune from saved weights) restores them."""
+    from ctgb import unet, warmstart as ws
+    net = unet.UNet3D(seed=5, device="cpu")
+    g = torch.Generator().manual_seed(1)
+    net.params["head.w"] = torch.randn(32, generator=g)
+    path = tmp_path / "w.npz"
+    ws.save(net, path, pairs=3, note="test")
+    back = ws.load(path, device="cpu")
+    for k, v in net.params.items():
+        assert torch.equal(back.params[k], v.to(torch.bfloat16).float()), k
+    assert "note" in str(np.load(path)["meta"])
