@@ -164,13 +164,14 @@ __global__ void up2_bwd_kernel(const bf16 *__restrict__ dout, bf16 *__restrict__
 
 // [n][z][y][x][c] -> three channel-major copies [n][ctot][z][y][x] at channel
 // offset coff, shifted along x by -1, 0, +1 (zero outside); a null output is skipped.
-// Block: 32 x 8 threads, tile of 32 x positions x 32 channels of one (n, z, y) row.
+// Block: 32 x 8 threads, tile of 32 x positions x 32 channels of one (n, z, y)
+// row; grid (rows, x tiles, channel tiles), rows in x (up to 2^31 - 1).
 __global__ void __launch_bounds__(256)
 shift_t_kernel(const bf16 *__restrict__ in, bf16 *__restrict__ om, bf16 *__restrict__ o0, bf16 *__restrict__ op,
                int c, int ctot, int coff, int nx, int ny, int nz) {
     __shared__ float tile[34][33];
-    const int x0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-    const long long row = blockIdx.z;   // (n * nz + z) * ny + y
+    const int x0 = blockIdx.y * 32, c0 = blockIdx.z * 32;
+    const long long row = blockIdx.x;   // (n * nz + z) * ny + y
     const long long nzy = (long long)nz * ny;
     const long long n = row / nzy, zy = row % nzy;
     const bf16 *src = in + row * nx * c;
@@ -347,8 +348,8 @@ int ct_unet_shift_t(const void *in, int c, int nb, int nz, int ny, int nx, void 
     CT_REQUIRE(nb > 0 && nz > 0 && ny > 0 && nx > 0, "shift_t: empty volume");
     const long long rows = (long long)nb * nz * ny;
     CT_REQUIRE(rows < (1ll << 31), "shift_t: volume too large");
-    dim3 grid((nx + 31) / 32, (c + 31) / 32, static_cast<unsigned>(rows));
-    CT_REQUIRE(grid.y <= 65535, "shift_t: too many channels");
+    dim3 grid(static_cast<unsigned>(rows), (nx + 31) / 32, (c + 31) / 32);
+    CT_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "shift_t: x or channel count too large");
     shift_t_kernel<<<grid, dim3(32, 8), 0, as_stream(stream)>>>(
         static_cast<const bf16 *>(in), static_cast<bf16 *>(om), static_cast<bf16 *>(o0), static_cast<bf16 *>(op), c,
         ctot, coff, nx, ny, nz);

@@ -134,6 +134,20 @@ def test_conv3d_wgrad_matches_autograd(cins, cout, taps, nb, nz, ny, nx, kper):
 
 
 @pytest.mark.gpu
+def test_shift_copies_past_65535_rows():
+    """The channel-major x-shifted copies for more than 65535 (n, z, y) rows
+    (a 256^3 training volume has 65536)."""
+    from ctgb import unet
+    g = torch.Generator(device="cuda").manual_seed(12)
+    t = torch.randn((1, 64, 1040, 8, 32), device="cuda", generator=g).to(BF)
+    xm, x0, xp = unet.shift_copies([t])
+    ref = t.permute(0, 4, 1, 2, 3)                                   # [n][c][z][y][x]
+    assert torch.equal(x0, ref)
+    assert torch.equal(xm[..., 1:], ref[..., :-1]) and torch.count_nonzero(xm[..., 0]) == 0
+    assert torch.equal(xp[..., :-1], ref[..., 1:]) and torch.count_nonzero(xp[..., -1]) == 0
+
+
+@pytest.mark.gpu
 def test_elementwise_ops_match_torch():
     import torch.nn.functional as F
     from ctgb import unet
