@@ -106,3 +106,12 @@ def test_weights_round_trip_through_save_and_load(tmp_path):
     for k, v in net.params.items():
         assert torch.equal(back.params[k], v.to(torch.bfloat16).float()), k
     assert "note" in str(np.load(path)["meta"])
+
+
+def test_time_to_residual_reads_the_first_check_at_or_below_tol():
+    from types import SimpleNamespace
+    from ctgb import warmstart as ws
+    run = SimpleNamespace(residuals=[(1, 0.3), (2, 0.2), (3, 0.1), (4, 0.05)], times=[0.5, 1.0, 1.5, 2.0])
+    assert ws.time_to_residual(run, 0.1) == (3, 1.5)
+    assert ws.time_to_residual(run, 0.1, t_start=0.25) == (3, 1.75)
+    assert ws.time_to_residual(run, 0.01) is None
