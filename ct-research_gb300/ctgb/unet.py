@@ -248,6 +248,9 @@ class UNet3D:
         """x: fp32 [n][z][y][x] (sizes multiples of 16) -> fp32 of the same shape."""
         if x.dim() == 3:
             x = x.unsqueeze(0)
+        if x.dim() != 4 or any(d % 16 for d in x.shape[1:]):
+            raise ValueError(f"U-Net input must be [n][z][y][x] with sizes multiples of 16 (three 2x poolings, "
+                             f"8-voxel tiles at the coarsest level); got {tuple(x.shape)}")
         x = x.contiguous()
         a = {"x": x}
         a["g"] = im2col27(x)

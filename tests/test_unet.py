@@ -253,3 +253,10 @@ def test_training_steps_reduce_loss():
     torch.cuda.synchronize()
     assert unet.status() == 0
     assert min(losses[-5:]) < 0.6 * losses[0], losses
+
+
+def test_network_rejects_sizes_it_cannot_pool():
+    from ctgb import unet
+    net = unet.UNet3D(seed=0, device="cpu")
+    with pytest.raises(ValueError, match="multiples of 16"):
+        net.forward(torch.zeros((1, 24, 32, 32)))
