@@ -245,7 +245,8 @@ class UNet3D:
                       x2=xs[1] if len(xs) > 1 else None, ntaps=ntaps)
 
     def forward(self, x: torch.Tensor, keep: bool = False):
-        """x: fp32 [n][z][y][x] (sizes multiples of 16) -> fp32 of the same shape."""
+        """x: fp32 [n][z][y][x] or [z][y][x] (sizes multiples of 16) -> fp32 [n][z][y][x].
+        keep=True saves the activations for backward()."""
         if x.dim() == 3:
             x = x.unsqueeze(0)
         if x.dim() != 4 or any(d % 16 for d in x.shape[1:]):
