@@ -87,9 +87,12 @@ def train(net: unet.UNet3D, pairs: PairSet, epochs: int = 4, lr: float = 3e-4, l
     cosine learning-rate decay from lr to lr_end; returns the mean loss per epoch.
 
     Each step flips the pair along a random subset of the axes and may swap x
-    and y: the 90-view set (multiples of 4 degrees) and the source orbit in the
-    central plane are unchanged by these, so the flipped pair is another valid
-    (FDK, SIRT-TV) pair of the same scan."""
+    and y.  A flip of x or y maps the view angles b to -b or pi - b, which keeps
+    the 90-view set (multiples of 4 degrees), and a flip of z keeps the central
+    orbit: the flipped pair is another (FDK, SIRT-TV) pair of the same scan.
+    The x-y swap maps b to 3 pi / 2 - b, i.e. the same scan with its views
+    turned by half a view step (2 degrees): still a 90-view pair of this
+    geometry."""
     n_pairs = pairs.inputs.shape[0]
     total = epochs * n_pairs
     rng = np.random.default_rng(seed)

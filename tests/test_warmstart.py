@@ -115,3 +115,27 @@ def test_time_to_residual_reads_the_first_check_at_or_below_tol():
     assert ws.time_to_residual(run, 0.1) == (3, 1.5)
     assert ws.time_to_residual(run, 0.1, t_start=0.25) == (3, 1.75)
     assert ws.time_to_residual(run, 0.01) is None
+
+
+def test_flip_augmentations_map_the_view_set_as_documented():
+    """x / y flips of the volume map the source angle b to -b / pi - b and keep
+    the 90-view set; the x-y swap maps b to 3 pi / 2 - b, the set turned by half
+    a view step."""
+    from ctgb import warmstart as ws
+    g = ws.scan(128, 90)
+    deg = np.round(np.degrees(g.beta.astype(np.float64)), 3) % 360.0     # float32 angles, to 0.001 degree
+    base = set(deg)
+    assert len(base) == 90 and all(d % 4 == 0 for d in deg)
+
+    def mapped(f):
+        return set(np.round(f(deg), 3) % 360.0)
+
+    assert mapped(lambda b: -b) == base                      # x flip: source (C_t - D sin b) mirrored
+    assert mapped(lambda b: 180.0 - b) == base               # y flip: source (C_s + D cos b) mirrored
+    swapped = mapped(lambda b: 270.0 - b)                    # x-y swap
+    assert swapped == set(np.round(deg + 2.0, 3) % 360.0)
+    # the mirrored source positions are those of the mapped angles
+    b = np.radians(deg)
+    for f, sx, sy in ((lambda v: -v, -1, 1), (lambda v: np.pi - v, 1, -1)):
+        assert np.allclose(sx * -np.sin(b), -np.sin(f(b))) and np.allclose(sy * np.cos(b), np.cos(f(b)))
+    assert np.allclose(np.cos(b), -np.sin(1.5 * np.pi - b)) and np.allclose(-np.sin(b), np.cos(1.5 * np.pi - b))
