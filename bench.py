@@ -172,7 +172,11 @@ def run_reference(args):
                              "sample": f"FP64 oracle (reference algorithm restated in C, OpenMP) FP+BP of {nv} "
                                        f"of the 360 views per step; the reference's own code is MATLAB + CUDA "
                                        f"MEX and cannot run on this host"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            # the metric's second half compares a learned start with plain SIRT-TV on the same GPU;
+            # the reference has no learned start, and its SIRT-TV is a MATLAB loop
+            "sirt_tv_learned_vs_plain": {"unavailable": "the reference has no learned warm start; its SIRT-TV "
+                                                        "is a MATLAB script over the MEX operators"}}
     print(json.dumps(line), flush=True)
 
 
