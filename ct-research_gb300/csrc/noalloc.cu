@@ -12,20 +12,25 @@
 // filtered sinogram -- lives in g_fbp_scratch, a file-scope device array of
 // kNoAllocScratchBytes (8 MiB).  Every GPU that loads the library holds this
 // array until the process exits.  Sizes whose tables and filtered sinogram do
-// not fit are rejected with CT_ERR_ARG.  The small tables are computed on the
-// host into a static host buffer and copied in with cudaMemcpyAsync (a copy,
-// not an allocation).
+// not fit are rejected with CT_ERR_ARG.  The caller's angle and detector
+// arrays are copied into the array with cudaMemcpyAsync (a copy, not an
+// allocation) and a small kernel derives the tables from them there.
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress, with that device current; make that first call
-// before any stream capture.  Every call shares the one array and leaves its
-// contents behind (the filter kernel zeroes the rows it accumulates into), so
-// calls whose GPU work overlaps -- on different streams, or from different
-// host threads -- race on it: serialise them.
+// before any stream capture.  Under CUDA's lazy module loading (the default)
+// the array's memory is committed when this file's code is first used on a
+// device, i.e. by that first call: a caller that reserves the rest of device
+// memory afterwards should make one call first (or load modules eagerly,
+// CUDA_MODULE_LOADING=EAGER).  Every call shares the one array and leaves its
+// contents behind (the filter kernel zeroes the rows it accumulates into, the
+// table kernel rewrites every table), so calls whose GPU work overlaps -- on
+// different streams, or from different host threads -- race on it: serialise
+// them.
+#include <algorithm>
 #include <cmath>
-#include <cstring>
 #include <mutex>
-#include <vector>
+#include <string>
 
 #include "kernels.cuh"
 
@@ -38,12 +43,39 @@ constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_fbp_scratch[kNoAllocScratchBytes];
 
-// host staging of the small tables (static: no host allocation per call either)
-alignas(256) unsigned char g_host_stage[size_t(1) << 20];
 std::mutex g_noalloc_mutex;
 void *g_scratch_ptr[kMaxDevices] = {};
 
 size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+// The FBP tables from the caller's float angles and bins (already in the
+// scratch array): (sin, cos) of each angle as the float of the double sine
+// and cosine (a correctly rounded sinf / cosf but for astronomically rare
+// ties); the Shepp-Logan taps of GFunction (FBPfan.cu:6-19) and the weights
+// Rscan / sqrt(Rscan^2 + P^2) (FBPfan.cu:32), in double with the products and
+// sums rounded one by one as the host tables of the allocating path are.
+__global__ void __launch_bounds__(256)
+fbp_tables_kernel(const float *__restrict__ beta, int nb, const float *__restrict__ P, int np, float pint,
+                  double rscan, float2 *__restrict__ trig, float *__restrict__ G, double *__restrict__ w) {
+    const double x = __dmul_rn((double)pint, 3.141592653589793);
+    const double a = __dmul_rn(x, x);
+    const int n_all = max(nb, 2 * np - 1);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_all; i += gridDim.x * blockDim.x) {
+        if (i < nb) {
+            const double b = (double)beta[i];
+            trig[i] = make_float2((float)sin(b), (float)cos(b));
+        }
+        if (i < 2 * np - 1) {
+            const int n = abs(i - (np - 1));
+            const double den = __dadd_rn(__dmul_rn(4.0, __dmul_rn((double)n, (double)n)), -1.0);
+            G[i] = n == 0 ? (float)__ddiv_rn(1.0, a) : (float)__ddiv_rn(__ddiv_rn(-1.0, a), den);
+        }
+        if (i < np) {
+            const double p = (double)P[i];
+            w[i] = __ddiv_rn(rscan, __dsqrt_rn(__dadd_rn(__dmul_rn(rscan, rscan), __dmul_rn(p, p))));
+        }
+    }
+}
 
 // Device address of g_fbp_scratch on the current device (looked up once per device).
 int scratch_address(void **out) {
@@ -70,17 +102,20 @@ extern "C" int ct_FBPfan_noalloc(float *d_Display, const float *d_R, const float
                                  int s_length, double Rscan, void *stream) {
     CT_REQUIRE(d_Display && d_R && Pdomain && BetaScanRange && Size, "ct_FBPfan_noalloc: null argument");
     CT_REQUIRE(LBeta > 0 && LP >= 2 && t_length > 0 && s_length > 0, "ct_FBPfan_noalloc: sizes must be positive");
+    CT_REQUIRE((long long)t_length * s_length < (1LL << 31), "ct_FBPfan_noalloc: image larger than 2^31 pixels");
     CT_REQUIRE(Size[0] > 0 && Size[1] > 0, "ct_FBPfan_noalloc: Size must be positive");
     CT_REQUIRE(Rscan > 0.5 * std::sqrt(Size[0] * Size[0] + Size[1] * Size[1]),
                "ct_FBPfan_noalloc: Rscan must exceed the half diagonal of the image");
-    // scratch layout: [trig (float2 per view)][P (float)][taps (2LP-1 float)][weights (double)][filtered]
-    const size_t o_trig = 0;
-    const size_t o_p = align256(o_trig + sizeof(float2) * (size_t)LBeta);
-    const size_t o_g = align256(o_p + sizeof(float) * (size_t)LP);
+    // scratch layout: [angles (float)][P (float)][trig (float2 per view)][taps (2LP-1 float)][weights (double)]
+    // [filtered sinogram]
+    const size_t o_b = 0;
+    const size_t o_p = align256(o_b + sizeof(float) * (size_t)LBeta);
+    const size_t o_trig = align256(o_p + sizeof(float) * (size_t)LP);
+    const size_t o_g = align256(o_trig + sizeof(float2) * (size_t)LBeta);
     const size_t o_w = align256(o_g + sizeof(float) * (2 * (size_t)LP - 1));
     const size_t o_rc = align256(o_w + sizeof(double) * (size_t)LP);
     const size_t total = o_rc + sizeof(float) * (size_t)LBeta * LP;
-    if (total > kNoAllocScratchBytes || o_rc > sizeof(g_host_stage)) {
+    if (total > kNoAllocScratchBytes) {
         set_error("ct_FBPfan_noalloc: LBeta * LP too large for the 8 MiB scratch array (needs " +
                   std::to_string(total) + " bytes)");
         return CT_ERR_ARG;
@@ -114,23 +149,17 @@ extern "C" int ct_FBPfan_noalloc(float *d_Display, const float *d_R, const float
     g.p0 = Pdomain[0];
     g.psgn = Pdomain[LP - 1] < Pdomain[0] ? -1.0f : 1.0f;
 
-    // tables on the host: sinf/cosf of the float angles, taps of GFunction
-    // (FBPfan.cu:6-19) and the weights Rscan / sqrt(Rscan^2 + P^2) (FBPfan.cu:32)
-    unsigned char *h = g_host_stage;
-    std::memset(h, 0, o_rc);
-    float2 *trig = reinterpret_cast<float2 *>(h + o_trig);
-    for (int v = 0; v < LBeta; ++v) trig[v] = make_float2(sinf(BetaScanRange[v]), cosf(BetaScanRange[v]));
-    std::memcpy(h + o_p, Pdomain, sizeof(float) * (size_t)LP);
-    float *G = reinterpret_cast<float *>(h + o_g);
-    const double PI = 3.141592653589793;
-    for (int n = 0; n < LP; ++n) {
-        const double a = 1.0 * ((double)g.pint * PI) * ((double)g.pint * PI);
-        if (n == 0) G[LP - 1] = (float)(1.0 / a);
-        else G[LP - 1 - n] = G[LP - 1 + n] = (float)(-1.0 / a / (4 * (1.0 * n * n) - 1));
-    }
-    double *w = reinterpret_cast<double *>(h + o_w);
-    for (int p = 0; p < LP; ++p) w[p] = Rscan / std::sqrt(1.0 * Rscan * Rscan + 1.0 * Pdomain[p] * Pdomain[p]);
-    CT_CUDA(cudaMemcpyAsync(dev, h, o_rc, cudaMemcpyHostToDevice, st), "ct_FBPfan_noalloc: table upload");
+    // the caller's angles and bins into the array, then the tables from them
+    CT_CUDA(cudaMemcpyAsync(dev + o_b, BetaScanRange, sizeof(float) * (size_t)LBeta, cudaMemcpyHostToDevice, st),
+            "ct_FBPfan_noalloc: angle upload");
+    CT_CUDA(cudaMemcpyAsync(dev + o_p, Pdomain, sizeof(float) * (size_t)LP, cudaMemcpyHostToDevice, st),
+            "ct_FBPfan_noalloc: bin upload");
+    const int n_all = std::max(LBeta, 2 * LP - 1);
+    fbp_tables_kernel<<<(n_all + 255) / 256, 256, 0, st>>>(
+        reinterpret_cast<const float *>(dev + o_b), LBeta, reinterpret_cast<const float *>(dev + o_p), LP, g.pint,
+        Rscan, reinterpret_cast<float2 *>(dev + o_trig), reinterpret_cast<float *>(dev + o_g),
+        reinterpret_cast<double *>(dev + o_w));
+    CT_LAUNCH_CHECK("fbp_tables_kernel");
 
     g.trig_f = reinterpret_cast<const float2 *>(dev + o_trig);
     g.Pf = reinterpret_cast<const float *>(dev + o_p);
