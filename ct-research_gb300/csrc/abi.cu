@@ -40,14 +40,51 @@ int sm_count() {
     return n;
 }
 
-// List of grazing rays for the FP64 re-walk (ref_walk.cu); allocated on first use.
+// Grazing rays for the FP64 re-walk (ref_walk.cu), in one buffer allocated on
+// first use: the list of `cap` entries, the count, and, for launches of
+// `nrays` rays, the overflow bitmap (one bit per ray; 17.7 MB at 360 x 512 x
+// 768).  The buffer is zeroed whenever its layout changes, and the re-walk
+// clears every bit it drains, so the bitmap is all zeros between launches.
+// With nrays = 0 there is no bitmap and an overflow is only counted.
 constexpr int kGrazeCap = 1 << 16;
-static int graze_list(DevBuf &b, GrazeList &gl) {
-    int s = b.ensure(sizeof(unsigned long long) * kGrazeCap + sizeof(int) * 4);
-    if (s) return s;
-    gl.rays = b.as<unsigned long long>();
-    gl.count = reinterpret_cast<int *>(b.as<unsigned long long>() + kGrazeCap);
-    gl.cap = kGrazeCap;
+static int g_graze_cap = kGrazeCap;   // list entries of later allocations (ct_set_graze_list_capacity)
+
+struct GrazeBuf {
+    DevBuf buf;
+    int cap = 0;
+    long long words = -1;
+    void release() { buf.release(); cap = 0; words = -1; }
+};
+
+static int graze_list(GrazeBuf &b, GrazeList &gl, long long nrays, cudaStream_t st, int cap = 0) {
+    if (cap <= 0) cap = g_graze_cap;
+    const long long words = (nrays + 31) / 32;
+    const size_t need = sizeof(unsigned long long) * ((size_t)cap + 2) + sizeof(unsigned int) * (size_t)words;
+    if (need > b.buf.bytes || cap != b.cap || words != b.words) {
+        int s = b.buf.ensure(need);
+        if (s) return s;
+        CT_CUDA(cudaMemsetAsync(b.buf.ptr, 0, need, st), "graze list clear");
+        b.cap = cap;
+        b.words = words;
+    }
+    gl.rays = b.buf.as<unsigned long long>();
+    gl.count = gl.rays + cap;
+    gl.cap = cap;
+    gl.bits = nrays > 0 ? reinterpret_cast<unsigned int *>(gl.rays + cap + 2) : nullptr;
+    gl.nbits = nrays;
+    return CT_OK;
+}
+
+// Number of grazing rays of the buffer's last projection (a diagnostic; syncs the stream).
+static int graze_count(const GrazeBuf &b, long long *n, cudaStream_t st) {
+    CT_REQUIRE(n, "null count pointer");
+    *n = 0;
+    if (!b.buf.ptr) return CT_OK;
+    unsigned long long h = 0;
+    CT_CUDA(cudaMemcpyAsync(&h, b.buf.as<unsigned long long>() + b.cap, sizeof(h), cudaMemcpyDeviceToHost, st),
+            "graze count");
+    CT_CUDA(cudaStreamSynchronize(st), "graze count sync");
+    *n = (long long)h;
     return CT_OK;
 }
 
@@ -174,8 +211,9 @@ using namespace ct;
 // ---------------------------------------------------------------------------
 struct ct_cone_plan {
     ConeGeom g{};
-    DevBuf trig, vsrc, P, xi;
-    DevBuf quads, rcov, G, wtab, norms, graze, volT, volS, pwt, win, scan;
+    DevBuf trig, vsrc, P, xi, xtab;
+    DevBuf quads, rcov, G, wtab, norms, volT, volS, pwt, win, scan;
+    GrazeBuf graze;
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     FilterOpts filt;
@@ -184,7 +222,7 @@ struct ct_cone_plan {
     std::vector<float> hb, hp, hx;
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
-        trig.release(); vsrc.release(); P.release(); xi.release();
+        trig.release(); vsrc.release(); P.release(); xi.release(); xtab.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
         volT.release(); volS.release(); pwt.release(); win.release(); scan.release();
     }
@@ -193,22 +231,31 @@ struct ct_cone_plan {
 // CSR export shared by the cone and fan plans: count pass, grazing-list check,
 // scan, and the fill pass when arrays are given.
 template <class Launch>
-static int sysmat_common(Launch launch, DevBuf &graze, DevBuf &scan, long long nrows, long long *d_row_ptr,
+static int sysmat_common(Launch launch, GrazeBuf &graze, DevBuf &scan, long long nrows, long long *d_row_ptr,
                          int *d_col, float *d_val, long long cap, long long *nnz, cudaStream_t st) {
     CT_REQUIRE(d_row_ptr && nnz, "sysmat: null row pointer or nnz");
     CT_REQUIRE(nrows > 0 && nrows < (1LL << 31), "sysmat: row count out of range");
     CT_REQUIRE((d_col == nullptr) == (d_val == nullptr), "sysmat: give both d_col and d_val, or neither");
     GrazeList gl;
     int s;
-    if ((s = graze_list(graze, gl))) return s;
-    if ((s = launch(gl, false))) return s;
-    int ng = 0;
-    CT_CUDA(cudaMemcpyAsync(&ng, gl.count, sizeof(int), cudaMemcpyDeviceToHost, st), "graze count");
+    // count pass; when the grazing rays overflow the list, grow it to hold
+    // them all and count again (the walk visits the same rays every time).
+    // The next projection sees the changed layout and clears the buffer.
+    int gcap = g_graze_cap;
+    for (;;) {
+        if ((s = graze_list(graze, gl, 0, st, gcap))) return s;
+        if ((s = launch(gl, false))) return s;
+        unsigned long long ng = 0;
+        CT_CUDA(cudaMemcpyAsync(&ng, gl.count, sizeof(ng), cudaMemcpyDeviceToHost, st), "graze count");
+        CT_CUDA(cudaStreamSynchronize(st), "sysmat sync");
+        if (ng <= (unsigned long long)gcap) break;
+        CT_REQUIRE(ng < (1ULL << 31), "sysmat: more than 2^31 grazing rays");
+        gcap = (int)ng;
+    }
     if ((s = csr_scan(d_row_ptr, (int)nrows, &scan.ptr, &scan.bytes, st))) return s;
     long long total = 0;
     CT_CUDA(cudaMemcpyAsync(&total, d_row_ptr + nrows, sizeof(long long), cudaMemcpyDeviceToHost, st), "nnz");
     CT_CUDA(cudaStreamSynchronize(st), "sysmat sync");
-    CT_REQUIRE(ng <= gl.cap, "sysmat: more grazing rays than the re-walk list holds");
     *nnz = total;
     if (!d_col) return CT_OK;
     CT_REQUIRE(cap >= total, "sysmat: d_col / d_val hold fewer entries than the matrix has");
@@ -274,11 +321,20 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
         tr[v] = make_double2(sb, cb);
         vs[v] = ViewSrc{Size[0] / 2 - D * sb, Size[1] / 2 + D * cb, D * sb, D * cb};
     }
+    // row table of the backprojectors: (x - q(xi[x]), q(xi[x+1]) - x) with the
+    // reference's row quotient q(v) = |v - xi[0]| / XigamaInt in double
+    std::vector<float2> xt(std::max(nx - 1, 1));
+    for (int x = 0; x + 1 < nx; ++x) {
+        const double q0 = std::fabs((double)xi[x] - (double)xi[0]) / (double)g.xint;
+        const double q1 = std::fabs((double)xi[x + 1] - (double)xi[0]) / (double)g.xint;
+        xt[x] = make_float2((float)(x - q0), (float)(q1 - x));
+    }
     if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->vsrc, vs.data(), nb)) || (s = upload(pl->P, P, np)) ||
-        (s = upload(pl->xi, xi, nx))) {
+        (s = upload(pl->xi, xi, nx)) || (s = upload(pl->xtab, xt.data(), xt.size()))) {
         delete pl;
         return s;
     }
+    g.xtab = pl->xtab.as<float2>();
     g.trig = pl->trig.as<double2>();
     g.vsrc = pl->vsrc.as<ViewSrc>();
     g.P = pl->P.as<float>();
@@ -326,8 +382,10 @@ int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable) {
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
     return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
-           plan->graze.bytes + plan->volT.bytes + plan->volS.bytes;
+           plan->graze.buf.bytes + plan->volT.bytes + plan->volS.bytes;
 }
+
+static long long cone_rays(const ConeGeom &g) { return (long long)g.nb * g.nx * g.np; }
 
 // The two zero-padded copies of the volume the forward projector reads
 // (plan workspace, refreshed every call): [z][s][t] and [z][t][s] (for views
@@ -356,7 +414,9 @@ int ct_cone_fp(ct_cone_plan *plan, const float *d_vol, float *d_proj, void *stre
     GrazeList gl;
     const float *volS, *volT;
     int s;
-    if ((s = graze_list(plan->graze, gl)) || (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream)))) return s;
+    if ((s = graze_list(plan->graze, gl, cone_rays(plan->g), as_stream(stream))) ||
+        (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream))))
+        return s;
     return cone_fp_launch(plan->g, volS, volT, d_vol, d_proj, nullptr, nullptr, 0.0f, nullptr, 0, gl,
                           as_stream(stream));
 }
@@ -367,7 +427,9 @@ int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b
     GrazeList gl;
     const float *volS, *volT;
     int s;
-    if ((s = graze_list(plan->graze, gl)) || (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream)))) return s;
+    if ((s = graze_list(plan->graze, gl, cone_rays(plan->g), as_stream(stream))) ||
+        (s = fp_volumes(plan, d_vol, &volS, &volT, as_stream(stream))))
+        return s;
     return cone_fp_launch(plan->g, volS, volT, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
@@ -462,6 +524,17 @@ int ct_cone_sysmat(ct_cone_plan *plan, int view0, int nviews, long long *d_row_p
                          cap, nnz, st);
 }
 
+int ct_cone_plan_grazing_rays(const ct_cone_plan *plan, long long *n, void *stream) {
+    CT_REQUIRE(plan, "ct_cone_plan_grazing_rays: null plan");
+    return graze_count(plan->graze, n, as_stream(stream));
+}
+
+int ct_set_graze_list_capacity(int cap) {
+    CT_REQUIRE(cap >= 1 && cap <= (1 << 26), "ct_set_graze_list_capacity: capacity must be in [1, 2^26]");
+    g_graze_cap = cap;
+    return CT_OK;
+}
+
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream) {
     CT_REQUIRE(plan && segments, "ct_cone_count_segments: null argument");
     cudaStream_t st = as_stream(stream);
@@ -486,7 +559,8 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
 // ---------------------------------------------------------------------------
 struct ct_fan_plan {
     FanGeom g{};
-    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, graze, pwt, win, scan;
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, pwt, win, scan;
+    GrazeBuf graze;
     std::vector<float> hPf, hbf;
     FilterOpts filt;
     double wsum = 0.0;
@@ -590,6 +664,11 @@ int ct_fan_sysmat(ct_fan_plan *plan, long long *d_row_ptr, int *d_col, float *d_
                          st);
 }
 
+int ct_fan_plan_grazing_rays(const ct_fan_plan *plan, long long *n, void *stream) {
+    CT_REQUIRE(plan, "ct_fan_plan_grazing_rays: null plan");
+    return graze_count(plan->graze, n, as_stream(stream));
+}
+
 int ct_fan_plan_set_filter(ct_fan_plan *plan, int kind, int window_len) {
     CT_REQUIRE(plan, "plan is null");
     int s = check_filter_opts(kind, window_len);
@@ -612,7 +691,7 @@ int ct_fan_plan_set_short_scan(ct_fan_plan *plan, int enable) {
 int ct_fan_fp(ct_fan_plan *plan, const float *d_img, float *d_proj, void *stream) {
     CT_REQUIRE(plan && d_img && d_proj, "ct_fan_fp: null argument");
     GrazeList gl;
-    int s = graze_list(plan->graze, gl);
+    int s = graze_list(plan->graze, gl, (long long)plan->g.nb * plan->g.np, as_stream(stream));
     if (s) return s;
     return fan_fp_launch(plan->g, d_img, d_proj, nullptr, nullptr, 0.f, nullptr, 0, gl, as_stream(stream));
 }
@@ -621,7 +700,7 @@ int ct_fan_fp_residual(ct_fan_plan *plan, const float *d_img, const float *d_b, 
                        float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(plan && d_img && d_b && d_out && d_norms, "ct_fan_fp_residual: null argument");
     GrazeList gl;
-    int s = graze_list(plan->graze, gl);
+    int s = graze_list(plan->graze, gl, (long long)plan->g.nb * plan->g.np, as_stream(stream));
     if (s) return s;
     return fan_fp_launch(plan->g, d_img, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
@@ -720,6 +799,20 @@ int cached_cone_plan(ct_cone_plan **out, int nt, int ns, int nz, const double *S
 
 extern "C" {
 
+int ct_dropin_release(void) {
+    {
+        std::lock_guard<std::mutex> lk(g_dropin_mutex);
+        DropinState &st = dropin();
+        if (st.cone) ct_cone_plan_destroy(st.cone);
+        st.cone = nullptr;
+        st.vol.release();
+        st.proj.release();
+    }
+    iterfdk_release_cache();
+    fdkui_release_cache();
+    return CT_OK;
+}
+
 int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaScanRange, const float *Pdomain,
                          const float *Xigamadomain, int t_length, int s_length, int z_length, double Center_t,
                          double Center_s, double Center_z, int LBeta, int LP, int LXigama, double Distance,
@@ -799,7 +892,7 @@ static int fan2d_run(ct_fan_plan *pl, int which, const void *in, void *out, int 
     if (e != cudaSuccess) s = cuda_status(e, "H2D");
     if (!s) {
         GrazeList gl;
-        if (fp && !(s = graze_list(pl->graze, gl)))
+        if (fp && !(s = graze_list(pl->graze, gl, (long long)nsino, 0)))
             s = fan_fp_launch(g, a.as<float>(), b.ptr, nullptr, nullptr, 0.f, nullptr, 3, gl, 0);
         else if (which == 1) s = fan_bp_launch(g, a.as<float>(), b.as<float>(), 0, nullptr, 0, 0, 0, 0, false, 0);
         else s = ct_fan_fbp(pl, a.as<float>(), b.as<float>(), filter_mode, nullptr);
@@ -898,7 +991,8 @@ int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float
 struct ct_fan_batch {
     std::vector<ct_fan_plan *> plans;
     std::vector<BatchSlice> h;
-    DevBuf desc, graze;
+    DevBuf desc;
+    GrazeBuf graze;
     int fp_block = 128, bp_block = 128;
     int fp_blocks = 0, bp_blocks = 0;
     long long img_total = 0, sino_total = 0;
@@ -1005,10 +1099,15 @@ int ct_fan_batch_set_filter(ct_fan_batch *b, int kind, int window_len, int short
     return CT_OK;
 }
 
+int ct_fan_batch_grazing_rays(const ct_fan_batch *b, long long *n, void *stream) {
+    CT_REQUIRE(b, "ct_fan_batch_grazing_rays: null batch");
+    return graze_count(b->graze, n, as_stream(stream));
+}
+
 int ct_fan_batch_fp(ct_fan_batch *b, const float *d_img, float *d_proj, void *stream) {
     CT_REQUIRE(b && d_img && d_proj, "ct_fan_batch_fp: null argument");
     GrazeList gl;
-    int s = graze_list(b->graze, gl);
+    int s = graze_list(b->graze, gl, b->sino_total, as_stream(stream));
     if (s) return s;
     return fan_batch_fp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->fp_blocks, b->fp_block, d_img, d_proj,
                                nullptr, nullptr, 0.f, nullptr, 0, gl, as_stream(stream));
@@ -1018,7 +1117,7 @@ int ct_fan_batch_fp_residual(ct_fan_batch *b, const float *d_img, const float *d
                              float *d_out, double *d_norms, void *stream) {
     CT_REQUIRE(b && d_img && d_b && d_out && d_norms, "ct_fan_batch_fp_residual: null argument");
     GrazeList gl;
-    int s = graze_list(b->graze, gl);
+    int s = graze_list(b->graze, gl, b->sino_total, as_stream(stream));
     if (s) return s;
     return fan_batch_fp_launch(b->desc.as<BatchSlice>(), (int)b->h.size(), b->fp_blocks, b->fp_block, d_img, d_out,
                                d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));

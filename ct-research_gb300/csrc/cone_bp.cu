@@ -17,6 +17,16 @@
 // This trades HBM capacity (4x the sinogram, 2.3 GB at 360x512x768) for a
 // quarter of the load instructions on a load-issue-bound kernel.
 //
+// Interpolation follows the reference's discontinuous index rule exactly:
+// column floor(|P - P0| / PInt) and row floor(|xi - xi0| / XigamaInt), with
+// PInt and XigamaInt the spacing of the first two (float) samples and the
+// weights |P - P[i]| / PInt, |xi - xi[j]| / XigamaInt from the actual sample
+// values (Backprojection3D.cu:73-87).  Float samples drift from that implied
+// grid (by ~1e-3 mm across a 512-row detector), so an index one off changes a
+// weight by up to ~4e-3: the column coordinate is computed per column-view in
+// float-float (ffloat.cuh), and the row quotient, affine in z, is stepped in
+// 64-bit fixed point with a per-row table of the samples' own quotients.
+//
 // Threads own one (t, s) column and ZC consecutive z; the view loop runs
 // inside the thread with the ZC sums in registers, and each voxel is written
 // once at the end (no atomics, deterministic).  The fused SIRT variant writes
@@ -24,6 +34,7 @@
 #include <type_traits>
 
 #include "cone_geom.cuh"
+#include "ffloat.cuh"
 
 namespace ct {
 
@@ -143,10 +154,10 @@ template <int WMODE, bool UPDATE>
 __global__ void __launch_bounds__(BP_BX * BP_BY, CT_BP_MINB)
 cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict__ vol,
                const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
-    // detector-row coordinate pairs (xi[x], xi[x+1]) for the interpolation weights
-    extern __shared__ float2 xpair[];
+    // the row table (x - q(xi[x]), q(xi[x+1]) - x) of ConeGeom::xtab
+    extern __shared__ float2 xtab[];
     const int tid = threadIdx.x + BP_BX * threadIdx.y;
-    for (int x = tid; x < g.nx - 1; x += BP_BX * BP_BY) xpair[x] = make_float2(g.xi[x], g.xi[x + 1]);
+    for (int x = tid; x < g.nx - 1; x += BP_BX * BP_BY) xtab[x] = g.xtab[x];
     __syncthreads();
 
     const int ti = blockIdx.x * BP_BX + threadIdx.x;
@@ -154,22 +165,28 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
     const int z0 = blockIdx.z * BP_ZC;
     if (ti >= g.nt || si >= g.ns) return;
 
+    // voxel-centre coordinates relative to the rotation centre, exact to ~2^-48
+    const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
+    const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const ff iz02 = ff_from((z0 + 0.5) * g.res[2] - 0.5 * g.size[2]);
+    const ff D2 = ff_from(g.D), rz2 = ff_from(g.res[2]);
+    const ff ipint2 = ff_from(1.0 / (double)g.pint);
+    const ff xq2 = ff_from((double)g.xsgn / (double)g.xint);   // row quotient per mm of xi
+    const ff p02 = {g.p0, 0.0f}, x02 = {g.x0, 0.0f};
+
     const float rz = (float)g.res[2];
-    const float it = (float)((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
-    const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const float it = it2.hi, is = is2.hi;
     const float D = (float)g.D;
-    const float ipint = 1.0f / g.pint, ixint = 1.0f / g.xint;
+    const float ipint = 1.0f / g.pint;
     const float ht = 0.5f * (float)g.res[0], hs = 0.5f * (float)g.res[1], hz = 0.5f * rz;
     const float czf = (float)(0.5 * g.size[2]);
     const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);   // iz at z = 0
-    const float iz0 = fmaf((float)z0, rz, x_base);                    // iz of this thread's first z
+    const float iz0 = iz02.hi;                                         // iz of this thread's first z
     // largest |iz| of the thread's z range: decides whether z faces can limit the chord
     const float izmax = fmaxf(fabsf(iz0), fabsf(fmaf((float)(BP_ZC - 1), rz, iz0)));
     const float iz_vol = fabsf(x_base);   // largest |iz| of the volume
     const float irz = 1.0f / rz, iD = 1.0f / D;
     const long long vstride = (long long)g.nx * g.np;
-    const float x0s = g.x0, ixs = ixint;
-    const float sxs = g.xsgn;   // direction of the detector-row domain
 
     float acc[BP_ZC];
 #pragma unroll
@@ -178,10 +195,14 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
     for (int v = 0; v < g.nb; ++v) {
         const double2 tr = g.trig[v];
         const float sb = (float)tr.x, cb = (float)tr.y;
-        const float dect_t = fmaf(it, cb, is * sb);
-        const float dect_s = fmaf(is, cb, -it * sb);
-        const float lr = D * __frcp_rn(D - dect_s);
-        const float P = dect_t * lr;
+        // detector coordinates of the column in float-float: the reference's
+        // FP64 dect_t, dect_s, LengthRatio = D / (D - dect_s) and P = dect_t * LR
+        // (Backprojection3D.cu:28-37)
+        const ff dt2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
+        const ff ds2 = ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb));
+        const ff lr2 = ff_div(D2, ff_sub(D2, ds2));
+        const ff P2 = ff_mul(dt2, lr2);
+        const float dect_s = ds2.hi, lr = lr2.hi, P = P2.hi;
         bool pin = P >= g.minp && P < g.maxp;
         // xi(z) = iz(z) * lr; detector rows in range for z in [zlo, zhi]
         // xi(z) >= minx  <=>  z >= (minx / lr - x_base) / rz, with 1/lr = (D - dect_s) / D
@@ -189,19 +210,24 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         const float zlo_f = fmaf(g.minx, ilr, -x_base) * irz, zhi_f = fmaf(g.maxx, ilr, -x_base) * irz;
         int zlo = (int)ceilf(zlo_f);             // first z with xi >= minx
         int zhi = (int)ceilf(zhi_f) - 1;         // last z with xi < maxx
-        // FP32 rounding is ~3e-5 in z units and ~2e-5 mm in P: re-decide in FP64 near an edge
+        // FP32 rounding is ~3e-5 in z units: re-decide in FP64 near an edge
         const bool near_edge = fabsf(zlo_f - rintf(zlo_f)) < 2.5e-4f || fabsf(zhi_f - rintf(zhi_f)) < 2.5e-4f ||
                                fabsf(P - g.minp) < 2e-4f || fabsf(P - g.maxp) < 2e-4f;
         if (near_edge) range_fp64(g, ti, si, tr.x, tr.y, pin, zlo, zhi);
         if (!pin) continue;   // whole column off the detector for this view
         if (WMODE == W_FDK_STICKY && zhi < zlo) continue;
-        // detector column: index floor(|P - P0| / PInt), weights from the domain
-        // values (Backprojection3D.cu:73-83)
-        int p1 = (int)(fabsf(P - g.p0) * ipint);
-        p1 = min(max(p1, 0), g.np - 2);
-        const float wq1 = fabsf(P - __ldg(g.P + p1)) * ipint;        // weight of column p1+1
-        const float wq0 = fabsf(__ldg(g.P + p1 + 1) - P) * ipint;    // weight of column p1
+        // detector column floor(|P - P0| / PInt) and weights |P - P[p1]| / PInt,
+        // |P[p1+1] - P| / PInt from the domain values (Backprojection3D.cu:73-83)
+        const int p1 = min(max(ff_floor(ff_mul(ff_abs(ff_sub(P2, p02)), ipint2)), 0), g.np - 2);
+        const float pa = __ldg(g.P + p1), pb = __ldg(g.P + p1 + 1);
+        const float wq1 = fabsf(__fadd_rn(__fsub_rn(P2.hi, pa), P2.lo)) * ipint;   // weight of column p1+1
+        const float wq0 = fabsf(__fsub_rn(__fsub_rn(pb, P2.hi), P2.lo)) * ipint;   // weight of column p1
         const float4 *Qv = Q + (long long)v * vstride + p1;
+        // row quotient q(z) = |xi(z) - xi[0]| / XigamaInt, affine in z, as 64-bit
+        // fixed point (32 fraction bits): floor and weights follow the
+        // reference's FP64 values except within ~1e-8 of a row boundary
+        const long long dqf = ff_fixed32(ff_mul(ff_mul(rz2, lr2), xq2));
+        long long r = ff_fixed32(ff_mul(ff_sub(ff_mul(iz02, lr2), x02), xq2));
 
         float wv = 1.0f, mts = 0.0f, qq = 0.0f;
         int zend = zhi;           // last z that receives this view's value
@@ -232,40 +258,39 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         } else {
             wv = lr * lr * g.bint;
         }
-        // the chord factor 2 * mts folds into the detector-column weights; where
-        // a z face can limit the chord the factor becomes min(1, hz / (|iz| mts))
+        // the chord factor 2 * mts (or the FDK weight) folds into the detector-column
+        // weights; where a z face can limit the chord the factor becomes
+        // min(1, hz / (|iz| mts))
         const float c0 = (WMODE == W_CHORD) ? 2.0f * mts : wv;
-        // row weights (xi - xi[x1]) / dXi and (xi[x1+1] - xi) / dXi carry the domain
-        // direction and 1 / dXi, folded into the column weights too
-        const float cx = sxs * ixint;
-        const float wa = wq0 * c0 * cx, wb = wq1 * c0 * cx;
-        // row index |xi - xi0| / dXi = iz * ua + ub for z whose row is on the detector
-        const float ua = sxs * lr * ixs, ub = -sxs * x0s * ixs;
+        const float wa = wq0 * c0, wb = wq1 * c0;
+        // sticky FDK: z above zhi re-add the value at zhi (the row quotient stops there)
+        const int kz = zhi - z0;
+        if (WMODE == W_FDK_STICKY && kz < 0) r += (long long)kz * dqf;
         // z of this thread that take this view, as a bit mask over k
         const int klo = max(zlo - z0, 0), khi = min(((WMODE == W_FDK_STICKY) ? 0x7fff : zend) - z0, BP_ZC - 1);
         const unsigned inmask = (klo > khi) ? 0u
                                 : ((khi >= 31 ? 0xffffffffu : ((2u << khi) - 1u)) & ~((1u << klo) - 1u));
         auto body = [&](auto zlim) {
             constexpr bool ZLIM = decltype(zlim)::value;
+            long long rk = r;
 #pragma unroll
             for (int k = 0; k < BP_ZC; ++k) {
-                float iz = fmaf((float)k, rz, iz0);
-                if (WMODE == W_FDK_STICKY) {
-                    if (z0 + k > zhi) iz = fmaf((float)zhi, rz, x_base);
-                }
-                // an index outside [0, nx-2] (z off the detector, or a negative index
-                // wrapped by the unsigned compare) is clamped for the read only
-                const unsigned x1 = min((unsigned)(int)fmaf(iz, ua, ub), (unsigned)(g.nx - 2));
-                const float2 xd = xpair[x1];
-                const float e1 = fmaf(iz, lr, -xd.x);      // xi - xi[x1]: weight of row x1+1
-                const float e0 = fmaf(-iz, lr, xd.y);      // xi[x1+1] - xi: weight of row x1
+                if (k > 0) rk += (WMODE == W_FDK_STICKY && k > kz) ? 0LL : dqf;
+                // an index outside [0, nx-2] (z off the detector, or a negative
+                // quotient wrapped by the unsigned compare) is clamped for the read only
+                const unsigned x1 = min((unsigned)(int)(rk >> 32), (unsigned)(g.nx - 2));
+                const float fr = __uint2float_rn((unsigned)rk);          // fraction * 2^32
+                const float2 xt = xtab[x1];
+                const float w1 = fmaf(fr, 2.3283064365386963e-10f, xt.x);    // |w1|: weight of row x1+1
+                const float w0 = fmaf(fr, -2.3283064365386963e-10f, xt.y);   // |w0|: weight of row x1
                 const float4 q = __ldg(Qv + (int)x1 * g.np);
                 const float top = fmaf(wa, q.x, wb * q.y);
                 const float bot = fmaf(wa, q.z, wb * q.w);
-                const float val = fmaf(e0, top, e1 * bot);
+                const float val = fmaf(fabsf(w0), top, fabsf(w1) * bot);
                 float w;
                 if (WMODE == W_CHORD) {
                     // chord 2 * min(h_a / |d_a|) * |d|, d = (dt, ds, iz)
+                    const float iz = fmaf((float)k, rz, iz0);
                     const float d2 = fmaf(iz, iz, qq);
                     const float len = d2 * rsqrtf(d2);
                     w = ZLIM ? fminf(1.0f, hz / (fabsf(iz) * mts)) * len : len;

@@ -53,10 +53,7 @@ cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__r
         if (MODE == 2) {
             r2 = hit ? (float)w.nseg : 0.0f;   // exact: counts < 2^19
         } else {
-            if (hit && w.grazing) {
-                const int slot = atomicAdd(gl.count, 1);
-                if (slot < gl.cap) gl.rays[slot] = (unsigned long long)o;
-            }
+            if (hit && w.grazing) graze_push(gl, (unsigned long long)o, (unsigned long long)o);
             const float val = hit ? ray_integral<false>(w, use_t ? volT : vol, nmax) : 0.0f;
             if (MODE == 0) {
                 out[o] = val;
@@ -113,7 +110,7 @@ int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const
     dim3 block(FP_BX, FP_BY);
     dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, g.nb);
     CT_REQUIRE(g.nb <= 65535, "cone_fp: at most 65535 views per launch");
-    if (mode != 2) CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
+    if (mode != 2) CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     if (mode == 0)
         cone_fp_kernel<0><<<grid, block, 0, st>>>(g, vol, volT, out, nullptr, nullptr, 0.0f, nullptr, gl);
     else if (mode == 1)
@@ -121,7 +118,7 @@ int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const
     else
         cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0f, norms, gl);
     CT_LAUNCH_CHECK("cone_fp_kernel");
-    if (mode != 2) return cone_fixup_launch(g, volU, out, b, rowsum, eps, norms, mode, gl.rays, gl.count, gl.cap, st);
+    if (mode != 2) return cone_fixup_launch(g, volU, out, b, rowsum, eps, norms, mode, gl, st);
     return CT_OK;
 }
 

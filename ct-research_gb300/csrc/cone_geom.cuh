@@ -27,6 +27,11 @@ struct ConeGeom {
     float minp, maxp, minx, maxx;
     float p0, x0;            // P[0], xi[0]
     float psgn, xsgn;        // +1 for ascending domains, -1 for descending
+    // Row table of the backprojectors: for x < nx - 1, (x - q(xi[x]), q(xi[x+1]) - x)
+    // with q(v) = |v - xi[0]| / xint the reference's row quotient (in double);
+    // the bilinear row weights |xi - xi[x]| / xint and |xi[x+1] - xi| / xint of a
+    // point with quotient x + f are then |f + tab.x| and |tab.y - f|.
+    const float2 *xtab;
 };
 
 }  // namespace ct

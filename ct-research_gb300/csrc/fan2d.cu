@@ -21,10 +21,7 @@ fan_fp_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__
     if (active) {
         bool grazing;
         const float val = fan_ray_value(g, img, r, grazing);
-        if (grazing) {
-            const int slot = atomicAdd(gl.count, 1);
-            if (slot < gl.cap) gl.rays[slot] = (unsigned long long)r;
-        }
+        if (grazing) graze_push(gl, (unsigned long long)r, (unsigned long long)r);
         if (MODE == 0) {
             out[r] = (OutT)val;
         } else {
@@ -64,7 +61,7 @@ int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
     const long long nray = (long long)g.nb * g.np;
     const unsigned blocks = (unsigned)((nray + F2_BLOCK - 1) / F2_BLOCK);
-    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
+    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     if (mode == 0)
         fan_fp_kernel<float, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (float *)out, nullptr, nullptr, 0.f, nullptr, gl);
     else if (mode == 1)
@@ -72,8 +69,7 @@ int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b,
     else
         fan_fp_kernel<double, 0><<<blocks, F2_BLOCK, 0, st>>>(g, img, (double *)out, nullptr, nullptr, 0.f, nullptr, gl);
     CT_LAUNCH_CHECK("fan_fp_kernel");
-    return fan_fixup_launch(g, img, out, mode == 3, b, rowsum, eps, norms, mode == 1 ? 1 : 0, gl.rays, gl.count,
-                            gl.cap, st);
+    return fan_fixup_launch(g, img, out, mode == 3, b, rowsum, eps, norms, mode == 1 ? 1 : 0, gl, st);
 }
 
 // wmode: 0 BackprojectionFan2D weight, 1 FBPfan, 2 FBPpara

@@ -22,6 +22,7 @@
 // Detector interpolation: index floor(|P - P0| / PInt), weights from the
 // domain values (BackprojectionFan2D.cu:44-53).
 #pragma once
+#include "ffloat.cuh"
 #include "kernels.cuh"
 #include "siddon.cuh"
 
@@ -66,35 +67,91 @@ __device__ __forceinline__ float fan_ray_value(const FanGeom &g, const float *__
     return ray_integral(w, img, g.nt * g.ns - 1);
 }
 
+// The reference's weight 2 |T1S1 - End| of one pixel-view in FP64
+// (BackprojectionFan2D.cu:56-114), each operation rounded on its own as the
+// reference's double arithmetic: End is the point 2 Rscan along the ray from
+// the source through the detector point pd (angle atan(pd / Rscan)), T1S1 the
+// line's crossing with the pixel's low t edge when its s lies in [0, s_high],
+// else with its low s edge when its t lies in [0, t_high]; 0 when neither (the
+// reference's thread returns).  Used where the FP32 tests lie within rounding
+// distance of those bounds.
+static __device__ __noinline__ float fan_chord_fp64(const FanGeom &g, int ti, int si, double sb, double cb, double pd) {
+    const double R = g.D, ct = 0.5 * g.size[0], cs = 0.5 * g.size[1];
+    const double src_t = __dsub_rn(ct, __dmul_rn(R, sb)), src_s = __dadd_rn(cs, __dmul_rn(R, cb));
+    const double th = atan(__ddiv_rn(pd, R));
+    const double smax = __dmul_rn(2.0, R);
+    const double st = __dmul_rn(smax, sin(th)), cr = __dsub_rn(R, __dmul_rn(smax, cos(th)));
+    const double end_t = __dsub_rn(__dadd_rn(ct, __dmul_rn(st, cb)), __dmul_rn(cr, sb));
+    const double end_s = __dadd_rn(__dadd_rn(cs, __dmul_rn(st, sb)), __dmul_rn(cr, cb));
+    const double dt = __dsub_rn(end_t, src_t), ds = __dsub_rn(end_s, src_s);
+    double t2s = __ddiv_rn(ds, dt == 0.0 ? __dadd_rn(dt, 1e-15) : dt);
+    double s2t = __ddiv_rn(dt, ds == 0.0 ? __dadd_rn(ds, 1e-15) : ds);
+    t2s = fmin(fmax(t2s, -1e16), 1e16);
+    s2t = fmin(fmax(s2t, -1e16), 1e16);
+    const double tlo = __dmul_rn((double)ti, g.res[0]), thi = __dmul_rn((double)(ti + 1), g.res[0]);
+    const double slo = __dmul_rn((double)si, g.res[1]), shi = __dmul_rn((double)(si + 1), g.res[1]);
+    const double tlo_s = __dadd_rn(src_s, __dmul_rn(__dsub_rn(tlo, src_t), t2s));
+    const double slo_t = __dadd_rn(src_t, __dmul_rn(__dsub_rn(slo, src_s), s2t));
+    double T1, S1;
+    if (tlo_s >= 0.0 && tlo_s <= shi) {
+        T1 = tlo;
+        S1 = tlo_s;
+    } else if (slo_t >= 0.0 && slo_t <= thi) {
+        T1 = slo_t;
+        S1 = slo;
+    } else {
+        return 0.0f;
+    }
+    const double et = __dsub_rn(T1, end_t), es = __dsub_rn(S1, end_s);
+    return (float)__dmul_rn(2.0, __dsqrt_rn(__dadd_rn(__dmul_rn(et, et), __dmul_rn(es, es))));
+}
+
+// a >= b and a < b for a float-float value and a float bound
+__device__ __forceinline__ bool ff_ge(ff a, float b) { return a.hi > b || (a.hi == b && a.lo >= 0.0f); }
+__device__ __forceinline__ bool ff_lt(ff a, float b) { return a.hi < b || (a.hi == b && a.lo < 0.0f); }
+
 // Sum over all views for pixel i (t fastest) with the weighting WMODE.
+// The detector coordinate follows the reference's FP64 P / U in float-float
+// (ffloat.cuh): the bin is floor(|Pd - P0| / PInt) with PInt the spacing of
+// the first two samples and weights |Pd - P[i]| / PInt from the actual sample
+// values, a discontinuous rule (float samples drift from the implied grid, by
+// ~1e-3 mm over 1024 bins) that FP32 coordinates do not reproduce at large
+// detectors.
 template <int WMODE>
 __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__restrict__ R, int i) {
     const int ti = i % g.nt, si = i / g.nt;
-    const float it = (float)((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
-    const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
+    const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const ff Rs2 = ff_from(g.D), p02 = {g.p0, 0.0f};
+    const ff ipint2 = ff_from(1.0 / (double)g.pint);
     const float Rs = (float)g.D;
     const float ipint = 1.0f / g.pint;
     // pixel edges in world coordinates (BackprojectionFan2D.cu:82)
     const float tlo = (float)(ti * g.res[0]), thi_ = (float)((ti + 1) * g.res[0]);
     const float slo = (float)(si * g.res[1]), shi_ = (float)((si + 1) * g.res[1]);
     const float ct_ = (float)(0.5 * g.size[0]), cs_ = (float)(0.5 * g.size[1]);
+    // FP32 rounding of the edge tests is ~1e-5 of the scan's extent
+    const float tie_m = 4e-6f * (Rs + (float)(g.size[0] + g.size[1]));
     float acc = 0.0f;
     for (int v = 0; v < g.nb; ++v) {
         const float2 tr = g.trig_f[v];
         const float sb = tr.x, cb = tr.y;
-        const float P = fmaf(it, cb, is * sb);
-        float Pd = P, u = 1.0f;
+        const ff P2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
+        ff Pd2 = P2;
+        float u = 1.0f;
         if (WMODE != BP2_FBPPAR) {
-            const float S = fmaf(is, cb, -it * sb);
-            u = (Rs - S) / Rs;
-            Pd = P / u;
+            const ff S2 = ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb));
+            const ff u2 = ff_div(ff_sub(Rs2, S2), Rs2);
+            Pd2 = ff_div(P2, u2);
+            u = u2.hi;
         }
+        const float Pd = Pd2.hi;
         float val = 0.0f;
-        if (Pd >= g.minp && Pd < g.maxp) {
-            int p1 = (int)(fabsf(Pd - g.p0) * ipint);
-            p1 = min(max(p1, 0), g.np - 2);
-            const float w1 = fabsf(Pd - __ldg(g.Pf + p1)) * ipint;
-            const float w0 = fabsf(__ldg(g.Pf + p1 + 1) - Pd) * ipint;
+        if (ff_ge(Pd2, g.minp) && ff_lt(Pd2, g.maxp)) {
+            const int p1 = min(max(ff_floor(ff_mul(ff_abs(ff_sub(Pd2, p02)), ipint2)), 0), g.np - 2);
+            const float pa = __ldg(g.Pf + p1), pb = __ldg(g.Pf + p1 + 1);
+            const float w1 = fabsf(__fadd_rn(__fsub_rn(Pd, pa), Pd2.lo)) * ipint;
+            const float w0 = fabsf(__fsub_rn(__fsub_rn(pb, Pd), Pd2.lo)) * ipint;
             const float *Rv = R + (long long)v * g.np + p1;
             val = fmaf(w0, __ldg(Rv), w1 * __ldg(Rv + 1));
         }
@@ -105,18 +162,26 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
             const float ex = ex0 * inv, ey = ey0 * inv;
             const float st = ct_ - Rs * sb, ss = cs_ + Rs * cb;
             const float a_end = 2.0f * Rs;
-            float a;
+            float w;
             const float at = (tlo - st) / ex;
             const float s_at = fmaf(at, ey, ss);
-            if (s_at >= 0.0f && s_at <= shi_) {
-                a = at;
-            } else {
+            bool tie = fabsf(s_at) < tie_m || fabsf(s_at - shi_) < tie_m;
+            bool none = false;
+            float a = at;
+            if (!(s_at >= 0.0f && s_at <= shi_)) {
                 const float as = (slo - ss) / ey;
                 const float t_as = fmaf(as, ex, st);
-                if (t_as >= 0.0f && t_as <= thi_) a = as;
-                else continue;
+                tie = tie || fabsf(t_as) < tie_m || fabsf(t_as - thi_) < tie_m;
+                a = as;
+                none = !(t_as >= 0.0f && t_as <= thi_);
             }
-            acc = fmaf(val, 2.0f * fabsf(a_end - a), acc);
+            if (tie) {
+                w = fan_chord_fp64(g, ti, si, (double)sb, (double)cb, (double)Pd + (double)Pd2.lo);
+            } else {
+                if (none) continue;
+                w = 2.0f * fabsf(a_end - a);
+            }
+            acc = fmaf(val, w, acc);
         } else if (WMODE == BP2_FBPFAN) {
             acc += val / (u * u) * g.bint;
         } else {

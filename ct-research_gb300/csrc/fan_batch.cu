@@ -46,11 +46,8 @@ fan_batch_fp_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__r
     if (active) {
         bool grazing;
         const float val = fan_ray_value(g, img + sl[k].img_off, r, grazing);
-        if (grazing) {
-            const int slot = atomicAdd(gl.count, 1);
-            if (slot < gl.cap) gl.rays[slot] = ((unsigned long long)k << 40) | (unsigned long long)r;
-        }
         const long long o = sl[k].sino_off + r;
+        if (grazing) graze_push(gl, ((unsigned long long)k << 40) | (unsigned long long)r, (unsigned long long)o);
         if (MODE == 0) {
             out[o] = val;
         } else {
@@ -92,13 +89,13 @@ int fan_batch_fp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block,
                         const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
                         cudaStream_t st) {
     CT_REQUIRE(block >= 32 && block <= 512 && block % 32 == 0, "batch: block size must be a multiple of 32 <= 512");
-    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
+    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     if (mode == 0)
         fan_batch_fp_kernel<0><<<nblocks, block, 0, st>>>(d_sl, nsl, img, out, nullptr, nullptr, 0.f, nullptr, gl);
     else
         fan_batch_fp_kernel<1><<<nblocks, block, 0, st>>>(d_sl, nsl, img, out, b, rowsum, eps, norms, gl);
     CT_LAUNCH_CHECK("fan_batch_fp_kernel");
-    return fan_batch_fixup_launch(d_sl, img, out, b, rowsum, eps, norms, mode, gl.rays, gl.count, gl.cap, st);
+    return fan_batch_fixup_launch(d_sl, nsl, img, out, b, rowsum, eps, norms, mode, gl, st);
 }
 
 int fan_batch_bp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block, const float *R, float *img, int wmode,

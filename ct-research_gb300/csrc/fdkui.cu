@@ -236,6 +236,9 @@ fdkui_bp_kernel(const UIGeom g, const UIView *__restrict__ views, const double *
 // ---------------------------------------------------------------------------
 struct UIState {
     DevBuf beta, gama, tang, dgam, xi, xif, taps, views, rcov, R, disp;
+    void release() {
+        for (DevBuf *b : {&beta, &gama, &tang, &dgam, &xi, &xif, &taps, &views, &rcov, &R, &disp}) b->release();
+    }
 };
 std::mutex g_ui_mutex;
 UIState &ui_state() {
@@ -348,6 +351,12 @@ int ui_bp(UIState &S, const UIGeom &g, const float *d_rcov, double *d_disp, cuda
 }
 
 }  // namespace
+
+// Free the device buffers the drop-in keeps between calls (ct_dropin_release).
+void fdkui_release_cache() {
+    std::lock_guard<std::mutex> lk(g_ui_mutex);
+    ui_state().release();
+}
 
 }  // namespace ct
 

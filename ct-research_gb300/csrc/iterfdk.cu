@@ -173,6 +173,9 @@ iterfdk_kernel(const IfdkGeom g, const float *__restrict__ pic, const int *__res
 
 struct IfdkState {
     DevBuf trig, U, P, Pf, K, G, tab, pic, err;
+    void release() {
+        for (DevBuf *b : {&trig, &U, &P, &Pf, &K, &G, &tab, &pic, &err}) b->release();
+    }
 };
 std::mutex g_ifdk_mutex;
 IfdkState &ifdk_state() {
@@ -250,6 +253,12 @@ int iterfdk_run(const IfdkGeom &g, const float *d_pic, float *d_err, const float
 }
 
 }  // namespace
+
+// Free the device buffers the drop-in keeps between calls (ct_dropin_release).
+void iterfdk_release_cache() {
+    std::lock_guard<std::mutex> lk(g_ifdk_mutex);
+    ifdk_state().release();
+}
 
 }  // namespace ct
 

@@ -38,12 +38,28 @@ struct RowFilter {
 };
 
 // Rays that graze a grid plane, listed by the fast projectors for the FP64
-// re-walk of ref_walk.cu.  count is reset by the launcher.
+// re-walk of ref_walk.cu.  count is reset by the launcher and counts every
+// grazing ray, listed or not.  The first cap rays go to the list; the rest
+// set their bit in `bits` (one bit per ray of the launch, nbits of them),
+// which the re-walk drains and clears, so no grazing ray is ever left with
+// the FP32 walk's value.  bits may be null (system-matrix export): the host
+// then reads count and re-runs with a list that holds every ray.
 struct GrazeList {
     unsigned long long *rays;
-    int *count;
+    unsigned long long *count;
     int cap;
+    unsigned int *bits;
+    long long nbits;
 };
+
+#ifdef __CUDACC__
+// Record a grazing ray: `entry` in the list, or bit `bit` once the list is full.
+__device__ __forceinline__ void graze_push(const GrazeList &gl, unsigned long long entry, unsigned long long bit) {
+    const unsigned long long slot = atomicAdd(gl.count, 1ULL);
+    if (slot < (unsigned long long)gl.cap) gl.rays[slot] = entry;
+    else if (gl.bits) atomicOr(gl.bits + (bit >> 5), 1u << (bit & 31));
+}
+#endif
 
 // vol is [z][s][t] and volT the same volume as [z][t][s], read for views whose
 // detector rows run closer to the s axis; both point kFpPadSlices slices into
@@ -55,11 +71,9 @@ int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const
                    cudaStream_t st);
 int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStream_t st);
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
-                      float eps, double *norms, int mode, const unsigned long long *list, const int *count, int cap,
-                      cudaStream_t st);
+                      float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_double, const float *b,
-                     const float *rowsum, float eps, double *norms, int mode, const unsigned long long *list,
-                     const int *count, int cap, cudaStream_t st);
+                     const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 size_t cone_quads_bytes(const ConeGeom &g);
 int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, cudaStream_t st);
 int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting, const float *colsum,
@@ -76,14 +90,17 @@ int cone_sysmat_launch(const ConeGeom &g, int v0, int nv, long long *row_ptr, in
 int fan_sysmat_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
                       cudaStream_t st);
 int cone_sysmat_ref_launch(const ConeGeom &g, long long r0, long long *row_ptr, int *col, float *val, bool fill,
-                           const unsigned long long *list, const int *count, int cap, cudaStream_t st);
-int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill,
-                          const unsigned long long *list, const int *count, int cap, cudaStream_t st);
+                           const GrazeList &gl, cudaStream_t st);
+int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
+                          cudaStream_t st);
 // row_ptr[1..n] <- inclusive prefix sum of itself, row_ptr[0] <- 0; tmp is CUB scratch
 int csr_scan(long long *row_ptr, int n, void **tmp, size_t *tmp_bytes, cudaStream_t st);
 int tv_flow_launch(float *x, float *work, double *scratch, int nx, int ny, int nz, int iters, float step,
                    float eps, float lo, cudaStream_t st);
 int sq_diff_sum_launch(const float *a, const float *b, long long n, double *out, cudaStream_t st);
+// Free the device buffers the IterativeFDK / curved-FDK drop-ins cache between calls.
+void iterfdk_release_cache();
+void fdkui_release_cache();
 
 }  // namespace ct
 
@@ -102,8 +119,8 @@ int fan_batch_fp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block,
 int fan_batch_bp_launch(const BatchSlice *d_sl, int nsl, int nblocks, int block, const float *R, float *img, int wmode,
                         const float *colsum, float eps, float lambda, float lo, float hi, bool update,
                         cudaStream_t st);
-int fan_batch_fixup_launch(const BatchSlice *d_sl, const float *img, float *out, const float *b, const float *rowsum,
-                           float eps, double *norms, int mode, const unsigned long long *list, const int *count,
-                           int cap, cudaStream_t st);
+int fan_batch_fixup_launch(const BatchSlice *d_sl, int nsl, const float *img, float *out, const float *b,
+                           const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
+                           cudaStream_t st);
 
 }  // namespace ct

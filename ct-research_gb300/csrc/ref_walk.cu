@@ -233,15 +233,39 @@ __device__ double par_ray_ref(const FanGeom &g, const float *__restrict__ pic, d
     return ray;
 }
 
-// Re-walk the listed rays.  mode 0: out = A x;  mode 1: out = (b - A x) * scale
+// Visit every grazing ray the fast kernel recorded: the listed entries, and,
+// when the list overflowed, every bit of the overflow bitmap.  Each bitmap
+// word is cleared as it is read, so the bitmap is all zeros again for the
+// next launch.  Grid-stride over both; call with the whole grid.
+template <class OnEntry, class OnBit>
+__device__ __forceinline__ void graze_drain(const GrazeList &gl, OnEntry on_entry, OnBit on_bit) {
+    const unsigned long long cnt = *gl.count;
+    const long long n = (long long)min(cnt, (unsigned long long)gl.cap);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = tid; i < n; i += stride) on_entry(gl.rays[i]);
+    if (cnt > (unsigned long long)gl.cap && gl.bits) {
+        const long long nw = (gl.nbits + 31) >> 5;
+        for (long long w = tid; w < nw; w += stride) {
+            unsigned m = gl.bits[w];
+            if (!m) continue;
+            gl.bits[w] = 0u;
+            while (m) {
+                const int bit = __ffs(m) - 1;
+                m &= m - 1;
+                on_bit((unsigned long long)w * 32 + bit);
+            }
+        }
+    }
+}
+
+// Re-walk the recorded rays.  mode 0: out = A x;  mode 1: out = (b - A x) * scale
 // with norms[0] corrected by the change of the squared residual.
 __global__ void __launch_bounds__(64)
 cone_fixup_kernel(const ConeGeom g, const float *__restrict__ vol, float *__restrict__ out,
                   const float *__restrict__ b, const float *__restrict__ rowsum, float eps, double *norms, int mode,
-                  const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
-    const int n = min(*count, cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const unsigned long long r = list[i];
+                  const GrazeList gl) {
+    auto fix = [&](unsigned long long r) {
         const int p = (int)(r % g.np), x = (int)((r / g.np) % g.nx), v = (int)(r / ((unsigned long long)g.np * g.nx));
         const double2 tr = g.trig[v];
         const float val = cone_ray_ref(g, vol, tr.x, tr.y, g.P[p], g.xi[x]);
@@ -253,17 +277,16 @@ cone_fixup_kernel(const ConeGeom g, const float *__restrict__ vol, float *__rest
             out[r] = rr * sc;
             atomicAdd(norms, (double)rr * rr);   // the fast kernel left this ray out of the norm
         }
-    }
+    };
+    graze_drain(gl, fix, fix);
 }
 
 template <typename OutT>
 __global__ void __launch_bounds__(64)
 fan_fixup_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restrict__ out,
                  const float *__restrict__ b, const float *__restrict__ rowsum, float eps, double *norms, int mode,
-                 const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
-    const int n = min(*count, cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const unsigned long long r = list[i];
+                 const GrazeList gl) {
+    auto fix = [&](unsigned long long r) {
         const int p = (int)(r % g.np), v = (int)(r / g.np);
         const double2 tr = g.trig_d[v];
         const double val = g.parallel ? par_ray_ref(g, img, tr.x, tr.y, g.Pd[p]) : fan_ray_ref(g, img, tr.x, tr.y, g.Pd[p]);
@@ -275,18 +298,17 @@ fan_fixup_kernel(const FanGeom g, const float *__restrict__ img, OutT *__restric
             out[r] = (OutT)(rr * sc);
             atomicAdd(norms, (double)rr * rr);   // the fast kernel left this ray out of the norm
         }
-    }
+    };
+    graze_drain(gl, fix, fix);
 }
 
-// Batched slices: entries are (slice << 40) | ray.
+// Batched slices: list entries are (slice << 40) | ray; bitmap bits are the
+// ray's offset in the packed sinogram.
 __global__ void __launch_bounds__(64)
-fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, const float *__restrict__ img, float *__restrict__ out,
-                       const float *__restrict__ b, const float *__restrict__ rowsum, float eps, double *norms, int mode,
-                       const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
-    const int n = min(*count, cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int k = (int)(list[i] >> 40);
-        const unsigned long long r = list[i] & ((1ULL << 40) - 1);
+fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, int nsl, const float *__restrict__ img,
+                       float *__restrict__ out, const float *__restrict__ b, const float *__restrict__ rowsum,
+                       float eps, double *norms, int mode, const GrazeList gl) {
+    auto fix = [&](int k, unsigned long long r) {
         const FanGeom g = sl[k].g;
         const int p = (int)(r % g.np), v = (int)(r / g.np);
         const double2 tr = g.trig_d[v];
@@ -301,7 +323,17 @@ fan_batch_fixup_kernel(const BatchSlice *__restrict__ sl, const float *__restric
             out[o] = rr * sc;
             atomicAdd(norms + 2 * k, (double)rr * rr);   // left out by the fast kernel
         }
-    }
+    };
+    auto on_entry = [&](unsigned long long e) { fix((int)(e >> 40), e & ((1ULL << 40) - 1)); };
+    auto on_bit = [&](unsigned long long o) {
+        int lo = 0, hi = nsl - 1;   // last slice whose sinogram starts at or before o
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((unsigned long long)sl[mid].sino_off <= o) lo = mid; else hi = mid - 1;
+        }
+        fix(lo, o - (unsigned long long)sl[lo].sino_off);
+    };
+    graze_drain(gl, on_entry, on_bit);
 }
 
 // One CSR row from a reference walk: pieces of zero length are dropped and
@@ -332,74 +364,74 @@ struct CsrRow {
 // at row_ptr[row]; rows are ray - r0.
 __global__ void __launch_bounds__(64)
 cone_sysmat_ref_kernel(const ConeGeom g, long long r0, long long *__restrict__ row_ptr, int *__restrict__ col,
-                       float *__restrict__ val, bool fill, const unsigned long long *__restrict__ list,
-                       const int *__restrict__ count, int cap) {
-    const int n = min(*count, cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const unsigned long long r = list[i];
+                       float *__restrict__ val, bool fill, const GrazeList gl) {
+    auto row_of = [&](unsigned long long r) {
         const int p = (int)(r % g.np), x = (int)((r / g.np) % g.nx), v = (int)(r / ((unsigned long long)g.np * g.nx));
         const long long row = (long long)r - r0;
         const double2 tr = g.trig[v];
         CsrRow e{fill, col, val, fill ? row_ptr[row] : 0, 0, -1};
         cone_walk_ref(g, tr.x, tr.y, g.P[p], g.xi[x], e);
         if (!fill) row_ptr[row + 1] = e.n;
-    }
+    };
+    graze_drain(gl, row_of, row_of);
 }
 
 __global__ void __launch_bounds__(64)
 fan_sysmat_ref_kernel(const FanGeom g, long long *__restrict__ row_ptr, int *__restrict__ col, float *__restrict__ val,
-                      bool fill, const unsigned long long *__restrict__ list, const int *__restrict__ count, int cap) {
-    const int n = min(*count, cap);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const unsigned long long r = list[i];
+                      bool fill, const GrazeList gl) {
+    auto row_of = [&](unsigned long long r) {
         const int p = (int)(r % g.np), v = (int)(r / g.np);
         const double2 tr = g.trig_d[v];
         CsrRow e{fill, col, val, fill ? row_ptr[r] : 0, 0, -1};
         if (g.parallel) par_walk_ref(g, tr.x, tr.y, g.Pd[p], e);
         else fan_walk_ref(g, tr.x, tr.y, g.Pd[p], e);
         if (!fill) row_ptr[r + 1] = e.n;
-    }
+    };
+    graze_drain(gl, row_of, row_of);
 }
 
 }  // namespace
 
-int fan_batch_fixup_launch(const BatchSlice *d_sl, const float *img, float *out, const float *b, const float *rowsum,
-                           float eps, double *norms, int mode, const unsigned long long *list, const int *count,
-                           int cap, cudaStream_t st) {
-    fan_batch_fixup_kernel<<<64, 64, 0, st>>>(d_sl, img, out, b, rowsum, eps, norms, mode, list, count, cap);
+// The re-walk grids: four 64-thread blocks per SM, grid-stride over the list
+// and the overflow bitmap.  A launch with nothing
+// recorded reads the count and returns.
+static unsigned fixup_blocks() { return (unsigned)(4 * sm_count()); }
+
+int fan_batch_fixup_launch(const BatchSlice *d_sl, int nsl, const float *img, float *out, const float *b,
+                           const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
+                           cudaStream_t st) {
+    fan_batch_fixup_kernel<<<fixup_blocks(), 64, 0, st>>>(d_sl, nsl, img, out, b, rowsum, eps, norms, mode, gl);
     CT_LAUNCH_CHECK("fan_batch_fixup_kernel");
     return CT_OK;
 }
 
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
-                      float eps, double *norms, int mode, const unsigned long long *list, const int *count, int cap,
-                      cudaStream_t st) {
-    cone_fixup_kernel<<<64, 64, 0, st>>>(g, vol, out, b, rowsum, eps, norms, mode, list, count, cap);
+                      float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
+    cone_fixup_kernel<<<fixup_blocks(), 64, 0, st>>>(g, vol, out, b, rowsum, eps, norms, mode, gl);
     CT_LAUNCH_CHECK("cone_fixup_kernel");
     return CT_OK;
 }
 
 int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_double, const float *b,
-                     const float *rowsum, float eps, double *norms, int mode, const unsigned long long *list,
-                     const int *count, int cap, cudaStream_t st) {
+                     const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
     if (out_double)
-        fan_fixup_kernel<double><<<64, 64, 0, st>>>(g, img, (double *)out, b, rowsum, eps, norms, mode, list, count, cap);
+        fan_fixup_kernel<double><<<fixup_blocks(), 64, 0, st>>>(g, img, (double *)out, b, rowsum, eps, norms, mode, gl);
     else
-        fan_fixup_kernel<float><<<64, 64, 0, st>>>(g, img, (float *)out, b, rowsum, eps, norms, mode, list, count, cap);
+        fan_fixup_kernel<float><<<fixup_blocks(), 64, 0, st>>>(g, img, (float *)out, b, rowsum, eps, norms, mode, gl);
     CT_LAUNCH_CHECK("fan_fixup_kernel");
     return CT_OK;
 }
 
 int cone_sysmat_ref_launch(const ConeGeom &g, long long r0, long long *row_ptr, int *col, float *val, bool fill,
-                           const unsigned long long *list, const int *count, int cap, cudaStream_t st) {
-    cone_sysmat_ref_kernel<<<64, 64, 0, st>>>(g, r0, row_ptr, col, val, fill, list, count, cap);
+                           const GrazeList &gl, cudaStream_t st) {
+    cone_sysmat_ref_kernel<<<fixup_blocks(), 64, 0, st>>>(g, r0, row_ptr, col, val, fill, gl);
     CT_LAUNCH_CHECK("cone_sysmat_ref_kernel");
     return CT_OK;
 }
 
-int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill,
-                          const unsigned long long *list, const int *count, int cap, cudaStream_t st) {
-    fan_sysmat_ref_kernel<<<64, 64, 0, st>>>(g, row_ptr, col, val, fill, list, count, cap);
+int fan_sysmat_ref_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
+                          cudaStream_t st) {
+    fan_sysmat_ref_kernel<<<fixup_blocks(), 64, 0, st>>>(g, row_ptr, col, val, fill, gl);
     CT_LAUNCH_CHECK("fan_sysmat_ref_kernel");
     return CT_OK;
 }

@@ -65,8 +65,8 @@ cone_sysmat_kernel(const ConeGeom g, int v0, long long *__restrict__ row_ptr, in
     RayWalk w;
     const bool hit = ray_setup(g, v, p, x, false, w);
     if (hit && w.grazing) {          // walked by the FP64 reference walk
-        const int slot = atomicAdd(gl.count, 1);
-        if (slot < gl.cap) gl.rays[slot] = (unsigned long long)(((long long)v * g.nx + x) * g.np + p);
+        const unsigned long long r = (unsigned long long)(((long long)v * g.nx + x) * g.np + p);
+        graze_push(gl, r, r);
         if (!FILL) row_ptr[row + 1] = 0;
         return;
     }
@@ -83,8 +83,7 @@ fan_sysmat_kernel(const FanGeom g, long long *__restrict__ row_ptr, int *__restr
     RayWalk w;
     const bool hit = fan_ray_setup(g, r, w);
     if (hit && w.grazing) {
-        const int slot = atomicAdd(gl.count, 1);
-        if (slot < gl.cap) gl.rays[slot] = (unsigned long long)r;
+        graze_push(gl, (unsigned long long)r, (unsigned long long)r);
         if (!FILL) row_ptr[r + 1] = 0;
         return;
     }
@@ -97,24 +96,24 @@ fan_sysmat_kernel(const FanGeom g, long long *__restrict__ row_ptr, int *__restr
 int cone_sysmat_launch(const ConeGeom &g, int v0, int nv, long long *row_ptr, int *col, float *val, bool fill,
                        const GrazeList &gl, cudaStream_t st) {
     CT_REQUIRE(nv > 0 && nv <= 65535 && v0 >= 0 && v0 + nv <= g.nb, "sysmat: view range out of bounds");
-    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
+    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     dim3 block(SM_BX, SM_BY), grid((g.np + SM_BX - 1) / SM_BX, (g.nx + SM_BY - 1) / SM_BY, nv);
     if (fill) cone_sysmat_kernel<true><<<grid, block, 0, st>>>(g, v0, row_ptr, col, val, gl);
     else cone_sysmat_kernel<false><<<grid, block, 0, st>>>(g, v0, row_ptr, col, val, gl);
     CT_LAUNCH_CHECK("cone_sysmat_kernel");
     const long long r0 = (long long)v0 * g.nx * g.np;
-    return cone_sysmat_ref_launch(g, r0, row_ptr, col, val, fill, gl.rays, gl.count, gl.cap, st);
+    return cone_sysmat_ref_launch(g, r0, row_ptr, col, val, fill, gl, st);
 }
 
 int fan_sysmat_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
                       cudaStream_t st) {
-    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(int), st), "graze list reset");
+    CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     const long long rays = (long long)g.nb * g.np;
     const unsigned blocks = (unsigned)((rays + 127) / 128);
     if (fill) fan_sysmat_kernel<true><<<blocks, 128, 0, st>>>(g, row_ptr, col, val, gl);
     else fan_sysmat_kernel<false><<<blocks, 128, 0, st>>>(g, row_ptr, col, val, gl);
     CT_LAUNCH_CHECK("fan_sysmat_kernel");
-    return fan_sysmat_ref_launch(g, row_ptr, col, val, fill, gl.rays, gl.count, gl.cap, st);
+    return fan_sysmat_ref_launch(g, row_ptr, col, val, fill, gl, st);
 }
 
 int csr_scan(long long *row_ptr, int n, void **tmp, size_t *tmp_bytes, cudaStream_t st) {

@@ -75,14 +75,29 @@ __device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
     return ok != 0;
 }
 
-// Wait for the phase of the given parity; false after kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+// Wait for the phase of the given parity; false after limit_ns (kWaitNs).
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, unsigned long long limit_ns = kWaitNs) {
     if (mbar_try(b, parity)) return true;
     const unsigned long long t0 = global_ns();
     for (;;) {
         for (int i = 0; i < 256; ++i)
             if (mbar_try(b, parity)) return true;
-        if (global_ns() - t0 > kWaitNs) return false;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
+}
+
+// Flag bit of a bounded wait that gave up in wait_selftest_kernel.
+constexpr int kErrSelftest = 8;
+
+// One thread waits, through the convolutions' own bounded wait, on an
+// mbarrier that nothing arrives on; the wait gives up after limit_ns and sets
+// the error flag as a timed-out convolution does.  No copy or tensor-memory
+// operation is in flight, so the kernel simply returns.
+__global__ void __launch_bounds__(32) wait_selftest_kernel(unsigned long long limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        if (!mbar_wait(&bar, 0, limit_ns)) atomicOr(&g_unet_err, kErrSelftest);
     }
 }
 
@@ -753,6 +768,13 @@ int ct_unet_conv3d_wgrad(const void *xm, const void *x0, const void *xp, int cin
         case 128: return launch_wgrad<128>(mm, m0, mp, md, a, grid, st);
         default: return launch_wgrad<256>(mm, m0, mp, md, a, grid, st);
     }
+}
+
+int ct_unet_wait_selftest(long long limit_ns, void *stream) {
+    CT_REQUIRE(limit_ns >= 1000 && limit_ns <= 1000000000LL, "unet_wait_selftest: limit must be in [1 us, 1 s]");
+    wait_selftest_kernel<<<1, 32, 0, as_stream(stream)>>>((unsigned long long)limit_ns);
+    CT_LAUNCH_CHECK("wait_selftest_kernel");
+    return CT_OK;
 }
 
 int ct_unet_status(int *flags) {

@@ -2,7 +2,9 @@
 
 Each .cu file compiles in parallel to an object, then one link step makes
 ``ctgb/_lib/libctgb.so``.  Only ``-gencode arch=compute_103a,code=sm_103a``
-is generated: the library is for GB300 only.
+is generated: the library is for GB300 only.  Two small host-only libraries
+carry the reference's own helper names with C++ linkage over it
+(include/ctgb_compat.h): ``libctgb_compat.so`` and ``libctgb_compat_bpfan.so``.
 """
 from __future__ import annotations
 
@@ -20,6 +22,7 @@ INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libctgb.so"
 OBJDIR = LIBDIR / "obj"
+COMPAT = {"libctgb_compat.so": [], "libctgb_compat_bpfan.so": ["-DCTGB_COMPAT_BPFAN"]}
 
 SOURCES = ["abi.cu", "cone_fp.cu", "cone_bp.cu", "filter.cu", "fan2d.cu", "sirt.cu", "ref_walk.cu", "fan_batch.cu",
            "noalloc.cu", "iterfdk.cu", "fdkui.cu", "sysmat.cu", "solvers.cu",
@@ -52,8 +55,24 @@ def _stale() -> bool:
     if not LIB.exists():
         return True
     t = LIB.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + [INCLUDE / "ctgb.h", Path(__file__)]
+    if any(not (LIBDIR / n).exists() or (LIBDIR / n).stat().st_mtime < t for n in COMPAT):
+        return True
+    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + [CSRC / "compat.cpp", INCLUDE / "ctgb.h",
+                                                                       INCLUDE / "ctgb_compat.h", Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps if p.exists())
+
+
+def _build_compat(exe: str) -> None:
+    """The reference-named C++ helpers, linked against libctgb.so (found next to them)."""
+    for name, defs in COMPAT.items():
+        out = LIBDIR / name
+        tmp = out.with_suffix(".so.tmp")
+        cmd = [exe, "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", f"-I{INCLUDE}", *defs,
+               str(CSRC / "compat.cpp"), "-o", str(tmp), f"-L{LIBDIR}", "-lctgb", "-Xlinker", "-rpath=$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compat build failed ({name}):\n{r.stderr}")
+        os.replace(tmp, out)
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> Path:
@@ -85,6 +104,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    _build_compat(exe)
     return LIB
 
 

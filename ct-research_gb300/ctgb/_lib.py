@@ -21,6 +21,7 @@ _fp, _dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
 SIGNATURES = {
     "ct_last_error": (C.c_char_p, []),
     "ct_version": (C.c_char_p, []),
+    "ct_dropin_release": (_i, []),
     "ct_ProjectionCone_3D": (_i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _d, _d, _i, _i, _i, _d, _vp]),
     "ct_BackPro": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _i, _i, _i, _vp, _i, _i, _i]),
     "ct_FDKpro": (_i, [_vp, _vp, _vp, _vp, _vp, _d, _i, _i, _i, _vp, _i, _i, _i]),
@@ -44,6 +45,10 @@ SIGNATURES = {
     "ct_cone_fdk_filter": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_fdk_bp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_count_segments": (_i, [_vp, C.POINTER(_ll), _vp]),
+    "ct_cone_plan_grazing_rays": (_i, [_vp, C.POINTER(_ll), _vp]),
+    "ct_fan_plan_grazing_rays": (_i, [_vp, C.POINTER(_ll), _vp]),
+    "ct_fan_batch_grazing_rays": (_i, [_vp, C.POINTER(_ll), _vp]),
+    "ct_set_graze_list_capacity": (_i, [_i]),
     "ct_cone_sysmat": (_i, [_vp, _i, _i, _vp, _vp, _vp, _ll, C.POINTER(_ll), _vp]),
     "ct_par_plan_create": (_i, [C.POINTER(_vp), _i, _i, _vp, _vp, _i, _vp, _i]),
     "ct_fan_sysmat": (_i, [_vp, _vp, _vp, _vp, _ll, C.POINTER(_ll), _vp]),
@@ -79,6 +84,7 @@ SIGNATURES = {
     "ct_unet_conv3d": (_i, [_vp, _i, _vp, _i, _i, _i, _i, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _i, _vp, _vp, _vp]),
     "ct_unet_conv3d_wgrad": (_i, [_vp, _vp, _vp, _i, _vp, _i, _i, _i, _i, _i, _i, _i, _vp, _vp]),
     "ct_unet_status": (_i, [C.POINTER(_i)]),
+    "ct_unet_wait_selftest": (_i, [_ll, _vp]),
     "ct_unet_im2col27": (_i, [_vp, _i, _i, _i, _i, _vp, _vp]),
     "ct_unet_pool2": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "ct_unet_pool2_bwd": (_i, [_vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _vp]),

@@ -149,6 +149,12 @@ class FanBatch:
         _lib.call("ct_fan_batch_fbp", self._h, _p(proj), _p(out), int(filter_mode), _stream())
         return out
 
+    def grazing_rays(self) -> int:
+        """Rays of the last forward projection that took the FP64 re-walk."""
+        n = C.c_longlong()
+        _lib.call("ct_fan_batch_grazing_rays", self._h, C.byref(n), _stream())
+        return int(n.value)
+
     def signature(self) -> str:
         h = hashlib.sha1()
         for g in self.geoms:

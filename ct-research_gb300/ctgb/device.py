@@ -48,6 +48,18 @@ def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def set_graze_list_capacity(cap: int) -> None:
+    """List capacity of grazing-ray buffers allocated from now on (process-wide;
+    the results do not depend on it: rays past the list take the overflow map)."""
+    _lib.call("ct_set_graze_list_capacity", int(cap))
+
+
+def _grazing(fn, h) -> int:
+    n = C.c_longlong()
+    _lib.call(fn, h, C.byref(n), _stream())
+    return int(n.value)
+
+
 class CsrMatrix:
     """A projector's system matrix in CSR on the device: row_ptr int64 (rows + 1),
     col int32, val float32 (segment lengths in mm)."""
@@ -181,6 +193,10 @@ class ConePlan:
         _lib.call("ct_cone_count_segments", self._h, C.byref(n), _stream())
         return int(n.value)
 
+    def grazing_rays(self) -> int:
+        """Rays of the last forward projection that took the FP64 re-walk."""
+        return _grazing("ct_cone_plan_grazing_rays", self._h)
+
     def workspace_bytes(self) -> int:
         return int(_lib.lib().ct_cone_plan_workspace_bytes(self._h))
 
@@ -251,6 +267,10 @@ class FanPlan:
         out = self.new_image(proj.device) if out is None else out
         _lib.call("ct_fan_fbp", self._h, _tptr(proj), _tptr(out), int(filter_mode), _stream())
         return out
+
+    def grazing_rays(self) -> int:
+        """Rays of the last forward projection that took the FP64 re-walk."""
+        return _grazing("ct_fan_plan_grazing_rays", self._h)
 
 
 class ParPlan(FanPlan):

@@ -61,6 +61,12 @@ def status() -> int:
     return flags.value
 
 
+def wait_selftest(limit_ns: int = 1_000_000) -> None:
+    """Queue a bounded mbarrier wait on a barrier nothing arrives on (it gives up
+    after ``limit_ns``); status() then raises CT_ERR_TIMEOUT with flag 8."""
+    _lib.call("ct_unet_wait_selftest", int(limit_ns), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
 # -- thin op wrappers ---------------------------------------------------------
 def conv3d(x1, w, bias=None, relu=False, x2=None, ntaps=27, split=None, masks=(None, None)):
     """Convolution of concat(x1, x2) (bf16 [n][z][y][x][c]) with w (bf16

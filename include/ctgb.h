@@ -40,6 +40,13 @@ typedef enum {
 const char *ct_last_error(void);
 /* Library version string. */
 const char *ct_version(void);
+/* Frees the device memory that the host-pointer entry points below keep
+ * between calls (the cone plan of the last geometry and its staging buffers,
+ * the IterativeFDK and curved-FDK buffers).  Call it before cudaDeviceReset,
+ * which the reference's gateways run after every call (ProjectionCone_3D.cpp:53):
+ * a reset frees those buffers behind the library's back.  No counterpart in
+ * the reference, whose helpers allocate and free on every call. */
+int ct_dropin_release(void);
 
 /* ===================================================================== */
 /* Drop-in host-pointer entry points.  Arguments, their meaning and the   */
@@ -105,12 +112,17 @@ int ct_FBPpara(float *Display, const float *R, const float *Tdomain, const float
 /* 2D fan FBP (as ct_FBPfan) that allocates no device memory; no counterpart in
  * the reference.  For callers that may not call cudaMalloc / cudaFree while they
  * run (memory reserved once at start-up, or a framework-owned device pool).
- * d_R (LBeta x LP sinogram) and d_Display (t x s image) are device buffers of the
- * caller; Pdomain, BetaScanRange and Size are host arrays.  All other data sits
- * in one library-owned 8 MiB device array: sizes that do not fit return
- * CT_ERR_ARG.  The first call on a device looks up that array's address; make it
- * before any stream capture.  Calls share the array, so calls that overlap on the
- * GPU race: serialise them.  Work is queued on `stream` (cudaStream_t). */
+ * d_R (LBeta x LP sinogram) and d_Display (t x s image, < 2^31 pixels) are
+ * device buffers of the caller; Pdomain, BetaScanRange and Size are host arrays,
+ * copied into the library's array with cudaMemcpyAsync on `stream`.  All other
+ * data sits in that one library-owned 8 MiB device array: sizes whose tables and
+ * filtered sinogram (about 4 * LBeta * LP bytes) do not fit return CT_ERR_ARG.
+ * The first call on a device looks up that array's address; make it before any
+ * stream capture.  Under CUDA's lazy module loading (the default) the array's
+ * 8 MiB are committed on a device by that first call, so a caller that reserves
+ * all remaining device memory should make one call before reserving.  Calls
+ * share the array, so calls that overlap on the GPU race: serialise them.  Work
+ * is queued on `stream` (cudaStream_t). */
 int ct_FBPfan_noalloc(float *d_Display, const float *d_R, const float *Pdomain,
                       const float *BetaScanRange, int LBeta, int LP, const double *Size, int t_length,
                       int s_length, double Rscan, void *stream);
@@ -194,6 +206,20 @@ int ct_cone_sysmat(ct_cone_plan *plan, int view0, int nviews, long long *d_row_p
 /* Exact number of Siddon segments over all rays of the plan (host result). */
 int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream);
 
+/* Rays that run along a grid plane to FP64 precision are re-walked with the
+ * reference's own FP64 walk (ProjectionCone_3D.cu:44-84 clamps their slopes
+ * at 1e16, and their charge follows that rounding).  The fast projector lists
+ * them for the re-walk; past the list's capacity (65536 by default) it marks
+ * them in a one-bit-per-ray overflow map that the re-walk drains, so every
+ * such ray gets the reference's value at any count.  These report how many
+ * rays of the plan's last forward projection took the re-walk (host result;
+ * synchronises `stream`).  No counterpart in the reference. */
+int ct_cone_plan_grazing_rays(const ct_cone_plan *plan, long long *n, void *stream);
+int ct_fan_plan_grazing_rays(const ct_fan_plan *plan, long long *n, void *stream);
+/* List capacity of grazing-ray buffers allocated from now on (process-wide;
+ * >= 1).  Memory tuning and tests; the results do not depend on it. */
+int ct_set_graze_list_capacity(int cap);
+
 /* 2D fan plan (ProjectionFan_2D / BackprojectionFan2D / FBPfan geometry). */
 int ct_fan_plan_create(ct_fan_plan **plan, int t_length, int s_length, const double *Size,
                        const double *BetaScanRange, int LBeta, const double *Pdomain, int LP,
@@ -248,6 +274,8 @@ int ct_fan_batch_bp_update(ct_fan_batch *batch, const float *d_proj, const float
 int ct_fan_batch_fbp(ct_fan_batch *batch, const float *d_proj, float *d_img, int filter_mode, void *stream);
 /* FBP filter options of every slice (ct_fan_plan_set_filter, ct_fan_plan_set_short_scan). */
 int ct_fan_batch_set_filter(ct_fan_batch *batch, int kind, int window_len, int short_scan);
+/* Grazing rays of the batch's last forward projection (as ct_fan_plan_grazing_rays). */
+int ct_fan_batch_grazing_rays(const ct_fan_batch *batch, long long *n, void *stream);
 
 /* ===================================================================== */
 /* IterativeFDK error slice                                               */
@@ -356,8 +384,14 @@ int ct_unet_conv3d(const void *d_x1, int c1, const void *d_x2, int c2, int nb, i
 int ct_unet_conv3d_wgrad(const void *d_xm, const void *d_x0, const void *d_xp, int cin, const void *d_dy, int cout,
                          int nb, int nz, int ny, int nx, int ntaps, int kper, float *d_dw, void *stream);
 /* Reads and clears the device flag of the convolutions' bounded waits:
- * CT_ERR_TIMEOUT (flags != 0) when a wait gave up since the last call. */
+ * CT_ERR_TIMEOUT (flags != 0) when a wait gave up since the last call.  Flag
+ * bits: 1 a free ring stage, 2 a loaded stage, 4 the last MMA, 8 the self-test. */
 int ct_unet_status(int *flags);
+/* Runs the convolutions' bounded mbarrier wait, with a limit of limit_ns
+ * (1 us .. 1 s), on a barrier that nothing arrives on: the wait gives up and
+ * sets flag 8, which ct_unet_status then reports as CT_ERR_TIMEOUT.  Shows that
+ * the bounded waits end and report; the context stays usable. */
+int ct_unet_wait_selftest(long long limit_ns, void *stream);
 /* out[v][k] = vol[v + off(k)] (k < 27, zero outside), 0 for k = 27..31: the
  * one-channel input as 32 channels for a 1-tap convolution. */
 int ct_unet_im2col27(const float *d_vol, int nb, int nz, int ny, int nx, void *d_out, void *stream);

@@ -35,7 +35,7 @@ def pytest_collection_modifyitems(config, items):
 @pytest.fixture(scope="session")
 def oracle():
     from oracle.oracle import Oracle
-    return Oracle(nthreads=min(8, os.cpu_count() or 1))
+    return Oracle(nthreads=os.cpu_count() or 1)
 
 
 @pytest.fixture(scope="session")

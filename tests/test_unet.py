@@ -260,3 +260,32 @@ def test_network_rejects_sizes_it_cannot_pool():
     net = unet.UNet3D(seed=0, device="cpu")
     with pytest.raises(ValueError, match="multiples of 16"):
         net.forward(torch.zeros((1, 24, 32, 32)))
+
+
+@pytest.mark.gpu
+def test_bounded_wait_gives_up_and_reports_timeout():
+    """A bounded mbarrier wait on a barrier that nothing arrives on gives up after
+    its limit (1 ms here), the host reads CT_ERR_TIMEOUT, the flag clears, and
+    the context keeps working: a convolution afterwards is still correct."""
+    import time
+    import torch.nn.functional as F
+    from ctgb import unet
+    from ctgb._lib import CTError
+    torch.cuda.synchronize()
+    assert unet.status() == 0
+    t0 = time.perf_counter()
+    unet.wait_selftest(1_000_000)
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 5.0
+    with pytest.raises(CTError) as e:
+        unet.status()
+    assert e.value.status == 5 and "flags 8" in str(e.value)
+    assert unet.status() == 0                     # read-and-clear
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.randn((1, 2, 8, 16, 32), device="cuda", generator=g).to(BF)
+    w = (torch.randn((32, 27, 32), device="cuda", generator=g) / np.sqrt(27 * 32)).to(BF)
+    out = unet.conv3d(x, w, torch.zeros(32, device="cuda"), relu=False)
+    torch.cuda.synchronize()
+    assert unet.status() == 0
+    ref = _t2ndhwc(F.conv3d(_ndhwc2t(x).float(), _w2torch(w.float()), None, padding=1)).to(BF)
+    assert rel_l2(out.float().cpu().numpy(), ref.float().cpu().numpy()) <= 2e-3
