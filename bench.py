@@ -8,8 +8,10 @@ rays = 360 * 768 * 512.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-N > 1 runs under torchrun, one rank per GPU, each rank a full replica of the
-workload (weak scaling: the views of a scan are independent units).
+N > 1 runs under torchrun, one rank per GPU: the scan's views are split over
+the ranks, each rank projects its views and backprojects them into a partial
+volume, and one NCCL all-reduce sums the volumes (strong scaling of one scan;
+ctgb.shard).  --replicas runs the whole scan on every rank instead (weak).
 The reference arm times the reference algorithm's CPU restatement (the FP64
 oracle, OpenMP over all host cores) on a bounded sample of the same workload.
 """
@@ -47,13 +49,14 @@ def _peaks():
 
 
 def _traffic():
+    """DRAM bytes per launch of the bench's kernels from the committed ncu summary
+    (profiles/traffic.json): kernel -> {"bytes_per_launch", "source"}."""
     p = ROOT / "profiles" / "traffic.json"
-    if p.exists():
-        try:
-            return json.loads(p.read_text())
-        except Exception:
-            return {}
-    return {}
+    try:
+        d = json.loads(p.read_text())
+    except Exception:
+        return {}
+    return {k: v for k, v in d.items() if isinstance(v, dict)}
 
 
 class ClockSampler:
@@ -180,6 +183,31 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def pair_parity(plan, geom, vol, proj, views=(44, 200)):
+    """rel-L2 of the timed FP and BP against the FP64 oracle on two views of the
+    workload, computed after the timed region: the FP on the phantom, the BP on
+    the FP's own output of those views (the oracle BP takes the same input)."""
+    import torch
+    from oracle.oracle import Oracle
+    o = Oracle(nthreads=os.cpu_count() or 1)
+    idx = [v for v in views if v < len(geom.beta)] or [0]
+    gs = geom.subset_views(idx)
+    fp = proj[idx].cpu().numpy()
+    t0 = time.perf_counter()
+    ref_fp = o.cone_fp(vol.cpu().numpy(), gs.beta, gs.P, gs.xi, gs.size, gs.D)
+    from ctgb.device import ConePlan
+    bp = ConePlan(gs).bp(proj[idx].contiguous()).cpu().numpy()
+    ref_bp = o.cone_bp(fp, gs.beta, gs.P, gs.xi, gs.size, gs.D, gs.vol_shape)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))
+
+    return {"fp_rel_l2_vs_oracle": rel(fp, ref_fp), "bp_rel_l2_vs_oracle": rel(bp, ref_bp),
+            "views": idx, "tolerance": 1e-5, "oracle": "FP64 C restatement of the reference kernels",
+            "seconds": time.perf_counter() - t0}
+
+
 def small_geometry():
     """Profiling case of the same kernels: 256^3, 90 views, 384x256 detector
     (volume 64 MiB, sinogram 35 MB: inputs above L2 together, one launch ~ms)."""
@@ -205,21 +233,47 @@ def run_ours(args):
     from ctgb.device import ConePlan
     ctgb.load()
     geom = geometry.config_cone_512() if args.size == "full" else small_geometry()
+    if args.views:
+        # profiling case: every k-th view of the scan (same volume, detector and per-view footprint)
+        geom = geom.subset_views(np.linspace(0, len(geom.beta) - 1, args.views).round().astype(int))
     vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2), device=dev)
+    scan = geom
+    sharded = world > 1 and not args.replicas
+    if sharded:
+        # one scan split by views over the ranks: FP of this rank's views, BP into a
+        # partial volume, one NCCL all-reduce of the volume (ctgb.shard)
+        from ctgb.shard import local_geometry
+        geom = local_geometry(scan, rank, world)
     plan = ConePlan(geom)
     proj = plan.new_sino(dev)
     back = plan.new_volume(dev)
     stream = torch.cuda.current_stream()
+    from ctgb.shard import ShardedPair
+
+    class _Timed:
+        """The plan's fp / bp with CUDA events on the launching stream around them."""
+        ev = None
+
+        def fp(self, v, out):
+            if self.ev:
+                self.ev[0].record(stream)
+            plan.fp(v, out)
+            if self.ev:
+                self.ev[1].record(stream)
+            return out
+
+        def bp(self, y, out):
+            plan.bp(y, out)
+            if self.ev:
+                self.ev[2].record(stream)
+            return out
+
+    timed = _Timed()
+    pair = ShardedPair(timed)
 
     def step(ev=None):
-        if ev:
-            ev[0].record(stream)
-        plan.fp(vol, proj)
-        if ev:
-            ev[1].record(stream)
-        plan.bp(proj, back)
-        if ev:
-            ev[2].record(stream)
+        timed.ev = ev
+        pair.step(vol, proj, back)
 
     for _ in range(max(args.warmup, 1)):
         step()
@@ -243,7 +297,8 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_total = float(t.item())
     t_step = t_total / args.steps
-    value = world * geom.n_rays / t_step / 1e9
+    job_rays = scan.n_rays if sharded else world * scan.n_rays
+    value = job_rays / t_step / 1e9
 
     # e2e through the C ABI with host (pinned) buffers: copies inside the timed region
     import ctypes as C
@@ -256,6 +311,8 @@ def run_ours(args):
     size = np.array(geom.size)
     vp = lambda a: C.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else C.c_void_p(a.data_ptr())
 
+    d_red = torch.empty(geom.vol_shape, dtype=torch.float32, device=dev) if sharded else None
+
     def e2e_step():
         _lib.check(lib.ct_ProjectionCone_3D(vp(h_vol), vp(h_proj), vp(geom.beta), vp(geom.P), vp(geom.xi),
                                             geom.nt, geom.ns, geom.nz, size[0] / 2, size[1] / 2, size[2] / 2,
@@ -264,6 +321,11 @@ def run_ours(args):
         _lib.check(lib.ct_BackPro(vp(h_back), vp(h_proj), vp(geom.xi), vp(geom.P), vp(geom.beta), geom.D,
                                   len(geom.beta), len(geom.P), len(geom.xi), vp(size), geom.nt, geom.ns, geom.nz),
                    "ct_BackPro")
+        if sharded:
+            # the partial volumes of the ranks' views summed into every rank's host volume
+            d_red.copy_(h_back, non_blocking=True)
+            dist.all_reduce(d_red)
+            h_back.copy_(d_red)
 
     if args.no_e2e:
         t_e2e = float("nan")
@@ -279,9 +341,9 @@ def run_ours(args):
         t = torch.tensor([t_e2e], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t_e2e = float(t.item())
-    e2e = {"value": world * geom.n_rays / t_e2e / 1e9, "unit": UNIT,
-           "h2d_bytes_per_step": int(h_vol.numel() * 4 + h_proj.numel() * 4),
-           "d2h_bytes_per_step": int(h_proj.numel() * 4 + h_back.numel() * 4),
+    e2e = {"value": job_rays / t_e2e / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_vol.numel() * 4 + h_proj.numel() * 4 + (h_back.numel() * 4 if sharded else 0)),
+           "d2h_bytes_per_step": int(h_proj.numel() * 4 + h_back.numel() * 4 * (2 if sharded else 1)),
            "ms_per_step": t_e2e * 1e3}
 
     if rank != 0:
@@ -304,13 +366,18 @@ def run_ours(args):
     }
     dom = "cone_fp_kernel" if t_fp >= t_bp else "cone_bp_kernel+pack_quads"
     ach = kern[dom]["achieved_gbs"]
-    tr = traffic.get(dom.split("+")[0]) if args.size == "full" else None
+    full_case = args.size == "full" and not args.views
+    tr = traffic.get(dom.split("+")[0]) if full_case else None
     roofline = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": tr, "kernel": dom, "peak_source": peak_kind,
+                "traffic": tr.get("bytes_per_launch") if isinstance(tr, dict) else tr,
+                "traffic_source": ("stored ncu capture of this kernel on this workload, not measured by this run: "
+                                   + tr.get("source", "profiles/traffic.json")) if isinstance(tr, dict) else None,
+                "kernel": dom, "peak_source": peak_kind,
                 "pair_frac": (fp_bytes + bp_bytes) / (t_fp + t_bp) / 1e9 / peak}
+    parity = None if args.no_parity else pair_parity(plan, geom, vol, proj)
     cpu = cpu_sample(geom, vol.cpu().numpy()) if (world == 1 and not args.no_cpu) else None
     warm = None
-    if world == 1 and args.size == "full" and not args.no_warmstart:
+    if world == 1 and full_case and not args.no_warmstart:
         # the metric's second half, measured after the timed region (1 GPU only)
         torch.cuda.empty_cache()
         w = measure_warmstart(500)
@@ -323,18 +390,22 @@ def run_ours(args):
                 "network_roofline": w["roofline"],
                 "workload": "512^3, 90 views, noise-free seed-7 phantom; target = the 500-iteration plain "
                             "SIRT-TV residual; times from the FDK volume, network included"}
-    if args.size != "full":
-        line_workload = f"{geom.name}: profiling case (not the benchmark workload)"
+    if not full_case:
+        line_workload = f"{geom.name}, {len(geom.beta)} views: profiling case (not the benchmark workload)"
     else:
         line_workload = WORKLOAD
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "strong" if sharded else "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": line_workload, "parallelism": f"replicas x{world}",
+            "config": {"workload": line_workload,
+                       "parallelism": (f"views split over {world} ranks, NCCL all-reduce of the volume" if sharded
+                                       else f"replicas x{world}"),
                        "l2": "inputs larger than L2 (512 MiB volume, 566 MB sinogram, 2.3 GB packed quads)",
                        "phantom": "12 random ellipsoids, seed 2"},
             "roofline": roofline, "kernels": kern, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "parity": parity,
             # per step: transpose_ts, cone_fp, cone_fixup, pack_quads, cone_bp (the ncu launch list)
             "gpu_launches": 5 * args.steps, "sirt_tv_learned_vs_plain": warm}
     print(json.dumps(line), flush=True)
@@ -769,6 +840,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI timing")
+    ap.add_argument("--no-parity", action="store_true", help="skip the rel-L2 check of the default line")
+    ap.add_argument("--replicas", action="store_true",
+                    help="N > 1: every rank runs the whole scan (weak scaling) instead of splitting its views")
+    ap.add_argument("--views", type=int, default=0,
+                    help="pair: use this many of the scan's views (profiling cases; not the benchmark line)")
     ap.add_argument("--no-warmstart", action="store_true",
                     help="skip the learned-vs-plain SIRT-TV measurement of the default line")
     ap.add_argument("--size", choices=["full", "small"], default="full",

@@ -77,6 +77,33 @@ def ellipsoids_3d(n_t: int, n_s: int, n_z: int, params: np.ndarray, device="cpu"
     return vol
 
 
+def phantom3d(n: int, ellipsoids, device="cpu") -> torch.Tensor:
+    """The voxel rule of phantom3d.m:71-108 on its own n^3 grid, returned in the
+    layout the reference's 3D scripts hand to the operators.
+
+    * Grid: voxel centres at ((0:n-1) - (n-1)/2) / ((n-1)/2), the end points
+      -1 and 1 included (phantom3d.m:73), not the cell centres of ellipsoids_3d.
+    * Rows (A, a, b, c, x0, y0, z0, phi) with phi in degrees about z
+      (phantom3d.m:87); a voxel gets the sum of the amplitudes of every
+      ellipsoid containing its centre, ((R (p - p0)) / (a, b, c))^2 summed <= 1,
+      R the rotation by phi; no clipping.
+    * Layout: meshgrid puts x along MATLAB's second index and y along the first,
+      and SIRT3D.m:51-57 vectorises pic(t, s, z) with t fastest, so the result is
+      float32 [z][s][t] with x along s and y along t."""
+    r = (torch.arange(n, device=device, dtype=torch.float64) - (n - 1) / 2.0) / ((n - 1) / 2.0)
+    y = r[None, None, :]          # t index
+    x = r[None, :, None]          # s index
+    z = r[:, None, None]          # z index
+    vol = torch.zeros(n, n, n, dtype=torch.float64, device=device)
+    for A, a, b, c_, x0, y0, z0, phi in ellipsoids:
+        ph = float(phi) * np.pi / 180.0
+        cp, sp = float(np.cos(ph)), float(np.sin(ph))
+        xr = cp * (x - x0) + sp * (y - y0)
+        yr = -sp * (x - x0) + cp * (y - y0)
+        vol += float(A) * ((xr / a) ** 2 + (yr / b) ** 2 + ((z - z0) / c_) ** 2 <= 1.0)
+    return vol.to(torch.float32)
+
+
 def world_ellipsoids(params: np.ndarray, size) -> list:
     """Normalised ellipsoid rows -> world-frame rows (A, a, b, c, x0, y0, z0, phi)
     in mm for a volume spanning [0, Size]; requires Size_t == Size_s so the

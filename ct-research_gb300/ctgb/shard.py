@@ -43,6 +43,23 @@ def allreduce_sum(t, group=None):
     return t
 
 
+class ShardedPair:
+    """One forward + back projection of a scan split by views over the ranks:
+    `plan` holds this rank's views (local_geometry).  fp writes this rank's
+    block of the sinogram (no exchange); bp backprojects that block into a
+    partial volume and one all-reduce (sum) makes every rank hold A^T y of the
+    whole scan.  With one rank it is the plain pair."""
+
+    def __init__(self, plan, group=None):
+        self.plan, self.group = plan, group
+
+    def step(self, vol, proj, back):
+        self.plan.fp(vol, proj)
+        self.plan.bp(proj, back)
+        allreduce_sum(back, self.group)
+        return proj, back
+
+
 class ShardedSirt:
     """SIRT over view shards: `plan` is this rank's plan over its views (anything
     with fp_residual / bp / fp / geom), `b` its block of the sinogram."""

@@ -76,11 +76,27 @@ def _worker(rank, world, port, result_path):
     fp_local = plan.fp(vol)
     # sharded backprojection: partial volumes summed over ranks
     bp = allreduce_sum(plan.bp(b[lo:hi].contiguous()))
+    # the bench's sharded pair: block of the sinogram and the all-reduced A^T A x
+    from ctgb.shard import ShardedPair
+    pair_proj, pair_back = torch.zeros(hi - lo, *g.sino_shape[1:]), torch.zeros(g.vol_shape)
+
+    class _OutPlan:                    # the oracle plan writing into given outputs, as ConePlan does
+        geom = plan.geom
+
+        def fp(self, v, out):
+            out.copy_(plan.fp(v))
+            return out
+
+        def bp(self, y, out):
+            out.copy_(plan.bp(y))
+            return out
+
+    ShardedPair(_OutPlan()).step(vol, pair_proj, pair_back)
     x = torch.zeros(g.vol_shape)
     sirt = ShardedSirt(plan, b[lo:hi].contiguous(), lam=1.0)
     r = [sirt.step(x) for _ in range(3)]
     np.savez(f"{result_path}_{rank}.npz", fp=fp_local.numpy(), bp=bp.numpy(), x=x.numpy(), r=np.array(r),
-             lo=lo, hi=hi)
+             lo=lo, hi=hi, pair_proj=pair_proj.numpy(), pair_back=pair_back.numpy())
     dist.destroy_process_group()
 
 
@@ -102,7 +118,10 @@ def test_two_rank_view_sharding_equals_single_process(tmp_path):
     # the two forward-projection blocks tile the full sinogram
     fp = np.concatenate([res[0]["fp"], res[1]["fp"]])
     assert np.array_equal(fp, b.numpy())
+    full_back = full.bp(full.fp(vol)).numpy()
+    assert np.array_equal(np.concatenate([res[0]["pair_proj"], res[1]["pair_proj"]]), b.numpy())
     for d in res:
+        assert np.linalg.norm(d["pair_back"] - full_back) <= 1e-6 * np.linalg.norm(full_back)
         assert np.linalg.norm(d["bp"] - bp_full) <= 1e-6 * np.linalg.norm(bp_full)
         assert np.linalg.norm(d["x"] - ref_x) <= 1e-5 * np.linalg.norm(ref_x)
     assert np.array_equal(res[0]["x"], res[1]["x"])
