@@ -234,8 +234,11 @@ def run_ours(args):
     ctgb.load()
     geom = geometry.config_cone_512() if args.size == "full" else small_geometry()
     if args.views:
-        # profiling case: every k-th view of the scan (same volume, detector and per-view footprint)
-        geom = geom.subset_views(np.linspace(0, len(geom.beta) - 1, args.views).round().astype(int))
+        # profiling case: every k-th view of the scan (same volume, detector and per-view footprint),
+        # or its first N views (--contiguous)
+        idx = np.arange(args.views) if args.contiguous else \
+            np.linspace(0, len(geom.beta) - 1, args.views).round().astype(int)
+        geom = geom.subset_views(idx)
     vol = phantom.ellipsoids_3d(geom.nt, geom.ns, geom.nz, phantom.ellipsoid_params(12, seed=2), device=dev)
     scan = geom
     sharded = world > 1 and not args.replicas
@@ -245,6 +248,8 @@ def run_ours(args):
         from ctgb.shard import local_geometry
         geom = local_geometry(scan, rank, world)
     plan = ConePlan(geom)
+    if args.bp_chunk:
+        plan.set_bp_chunk(args.bp_chunk)
     proj = plan.new_sino(dev)
     back = plan.new_volume(dev)
     stream = torch.cuda.current_stream()
@@ -406,8 +411,8 @@ def run_ours(args):
                        "phantom": "12 random ellipsoids, seed 2"},
             "roofline": roofline, "kernels": kern, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "parity": parity,
-            # per step: transpose_ts, cone_fp, cone_fixup, pack_quads, cone_bp (the ncu launch list)
-            "gpu_launches": 5 * args.steps, "sirt_tv_learned_vs_plain": warm}
+            # per step: transpose_ts, cone_fp, cone_fixup, then pack_quads + cone_bp per view chunk
+            "gpu_launches": plan.launches_per_pair() * args.steps, "sirt_tv_learned_vs_plain": warm}
     print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
@@ -843,6 +848,8 @@ def main():
     ap.add_argument("--no-parity", action="store_true", help="skip the rel-L2 check of the default line")
     ap.add_argument("--replicas", action="store_true",
                     help="N > 1: every rank runs the whole scan (weak scaling) instead of splitting its views")
+    ap.add_argument("--bp-chunk", type=int, default=0, help="pair: views per backprojection chunk (tuning)")
+    ap.add_argument("--contiguous", action="store_true", help="--views: the scan's first N views, not every k-th")
     ap.add_argument("--views", type=int, default=0,
                     help="pair: use this many of the scan's views (profiling cases; not the benchmark line)")
     ap.add_argument("--no-warmstart", action="store_true",

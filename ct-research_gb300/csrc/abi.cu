@@ -211,9 +211,10 @@ using namespace ct;
 // ---------------------------------------------------------------------------
 struct ct_cone_plan {
     ConeGeom g{};
-    DevBuf trig, vsrc, P, xi, xtab;
-    DevBuf quads, rcov, G, wtab, norms, volT, volS, pwt, win, scan;
+    DevBuf trig, vsrc, P, xi, xtab, vorder;
+    DevBuf quads, rcov, G, wtab, norms, volT, volS, pwt, win, scan, bpsum;
     GrazeBuf graze;
+    int bp_chunk = 0;   // views per backprojection chunk; 0: all views in one pass
     int fdk_filter = CT_FDK_FILTER_LAUNCH_ORDER;
     int fdk_bp = CT_FDK_BP_STICKY;
     FilterOpts filt;
@@ -222,9 +223,9 @@ struct ct_cone_plan {
     std::vector<float> hb, hp, hx;
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
-        trig.release(); vsrc.release(); P.release(); xi.release(); xtab.release();
+        trig.release(); vsrc.release(); P.release(); xi.release(); xtab.release(); vorder.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
-        volT.release(); volS.release(); pwt.release(); win.release(); scan.release();
+        volT.release(); volS.release(); pwt.release(); win.release(); scan.release(); bpsum.release();
     }
 };
 
@@ -329,12 +330,21 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
         const double q1 = std::fabs((double)xi[x + 1] - (double)xi[0]) / (double)g.xint;
         xt[x] = make_float2((float)(x - q0), (float)(q1 - x));
     }
+    // forward-projector view order: the views that read the [z][s][t] volume
+    // (detector columns closer to t: |cos b| >= |sin b|, as cone_fp_kernel
+    // picks) first, then those that read the [z][t][s] copy
+    std::vector<int> vo;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int v = 0; v < nb; ++v)
+            if ((std::fabs(tr[v].y) >= std::fabs(tr[v].x)) == (pass == 0)) vo.push_back(v);
     if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->vsrc, vs.data(), nb)) || (s = upload(pl->P, P, np)) ||
-        (s = upload(pl->xi, xi, nx)) || (s = upload(pl->xtab, xt.data(), xt.size()))) {
+        (s = upload(pl->xi, xi, nx)) || (s = upload(pl->xtab, xt.data(), xt.size())) ||
+        (s = upload(pl->vorder, vo.data(), vo.size()))) {
         delete pl;
         return s;
     }
     g.xtab = pl->xtab.as<float2>();
+    g.vorder = pl->vorder.as<int>();
     g.trig = pl->trig.as<double2>();
     g.vsrc = pl->vsrc.as<ViewSrc>();
     g.P = pl->P.as<float>();
@@ -382,7 +392,14 @@ int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable) {
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan) {
     if (!plan) return 0;
     return plan->quads.bytes + plan->rcov.bytes + plan->G.bytes + plan->wtab.bytes + plan->norms.bytes +
-           plan->graze.buf.bytes + plan->volT.bytes + plan->volS.bytes;
+           plan->graze.buf.bytes + plan->volT.bytes + plan->volS.bytes + plan->bpsum.bytes;
+}
+
+int ct_cone_plan_set_bp_chunk(ct_cone_plan *plan, int views) {
+    CT_REQUIRE(plan, "plan is null");
+    CT_REQUIRE(views >= 0, "views per backprojection chunk must be >= 0");
+    plan->bp_chunk = views;
+    return CT_OK;
 }
 
 static long long cone_rays(const ConeGeom &g) { return (long long)g.nb * g.nx * g.np; }
@@ -433,14 +450,34 @@ int ct_cone_fp_residual(ct_cone_plan *plan, const float *d_vol, const float *d_b
     return cone_fp_launch(plan->g, volS, volT, d_vol, d_out, d_b, d_rowsum, eps, d_norms, 1, gl, as_stream(stream));
 }
 
+// Backprojection in chunks of plan->bp_chunk views (0: all views at once):
+// every chunk is packed into quads and backprojected, its sums added to the
+// volume (or, for the fused SIRT update, to a partial-sum volume that the last
+// chunk folds into the update).
 static int cone_bp_common(ct_cone_plan *plan, const float *d_proj, float *d_vol, int weighting,
                           const float *colsum, float eps, float lambda, float lo, float hi, bool update,
                           cudaStream_t st) {
-    int s = plan->quads.ensure(cone_quads_bytes(plan->g));
+    const ConeGeom &g = plan->g;
+    const int chunk = plan->bp_chunk > 0 ? std::min(plan->bp_chunk, g.nb) : g.nb;
+    const int nchunks = (g.nb + chunk - 1) / chunk;
+    int s = plan->quads.ensure(cone_quads_bytes(g, chunk));
     if (s) return s;
-    if ((s = cone_pack_quads(plan->g, d_proj, plan->quads.as<float4>(), st))) return s;
-    return cone_bp_launch(plan->g, plan->quads.as<float4>(), d_vol, weighting, colsum, eps, lambda, lo, hi,
-                          update, st);
+    float *part = nullptr;
+    if (update && nchunks > 1) {
+        if ((s = plan->bpsum.ensure(sizeof(float) * (size_t)g.nt * g.ns * g.nz))) return s;
+        part = plan->bpsum.as<float>();
+    }
+    for (int c = 0; c < nchunks; ++c) {
+        const int v0 = c * chunk, nv = std::min(chunk, g.nb - v0);
+        const bool last = c == nchunks - 1;
+        if ((s = cone_pack_quads(g, d_proj, plan->quads.as<float4>(), v0, nv, st))) return s;
+        const float *prev = c == 0 ? nullptr : (update ? part : d_vol);
+        float *out = (update && !last) ? part : d_vol;
+        if ((s = cone_bp_launch(g, plan->quads.as<float4>(), v0, nv, prev, out, weighting, colsum, eps, lambda, lo,
+                                hi, update && last, st)))
+            return s;
+    }
+    return CT_OK;
 }
 
 int ct_cone_bp(ct_cone_plan *plan, const float *d_proj, float *d_vol, void *stream) {

@@ -50,6 +50,7 @@ constexpr int BP_BX = 32;          // t per block
 constexpr int BP_BY = 4;           // s per block
 constexpr int BP_ZC = CT_BP_ZC;    // z per thread (register accumulators)
 
+// Quads of nb views; R points at the first of them.
 __global__ void __launch_bounds__(256)
 pack_quads_kernel(const float *__restrict__ R, float4 *__restrict__ Q, int nb, int nx, int np) {
     const long long n = (long long)nb * nx * np;
@@ -126,16 +127,46 @@ __device__ __noinline__ bool chord_entry_found(const ConeGeom &g, int ti, int si
     return zlo_t >= tlo && zlo_t <= thi && zlo_s >= slo && zlo_s <= shi;
 }
 
+// The in-plane parts of the reference's first two face tests, which do not
+// depend on z (Backprojection3D.cu:262-270): the line from the source to the
+// voxel centre crosses the low t face within the voxel's s bounds, or the low
+// s face within its t bounds.  Same operations as chord_entry_found.
+__device__ __noinline__ bool chord_side_found(const ConeGeom &g, int ti, int si, double sb, double cb) {
+    const double EPS = 1e-15;
+    const double ct = g.size[0] / 2, cs = g.size[1] / 2;
+    const double rt = g.res[0], rs = g.res[1];
+    const double it = __dsub_rn(__dmul_rn(ti + 0.5, rt), ct);
+    const double is = __dsub_rn(__dmul_rn(si + 0.5, rs), cs);
+    const double st = __dsub_rn(ct, __dmul_rn(g.D, sb)), ss = __dadd_rn(cs, __dmul_rn(g.D, cb));
+    const double et = __dadd_rn(it, ct), es = __dadd_rn(is, cs);
+    const double tlo = __dmul_rn((double)ti, rt), thi = __dmul_rn((double)(ti + 1), rt);
+    const double slo = __dmul_rn((double)si, rs), shi = __dmul_rn((double)(si + 1), rs);
+    const double dt = __dsub_rn(et, st), ds = __dsub_rn(es, ss);
+    const double dte = __dadd_rn(dt, EPS), dse = __dadd_rn(ds, EPS);
+    const double tlo_s = __dadd_rn(ss, __ddiv_rn(__dmul_rn(__dsub_rn(tlo, st), ds), dte));
+    if (tlo_s >= slo && tlo_s <= shi) return true;
+    const double slo_t = __dadd_rn(st, __ddiv_rn(__dmul_rn(__dsub_rn(slo, ss), dt), dse));
+    return slo_t >= tlo && slo_t <= thi;
+}
+
 // Last z of a column that a view reaches when the source->centre line passes
 // near a voxel edge (two faces' chord parameters tie within FP32 margins): the
 // reference's FP64 face tests may then all fail at some z, and it returns,
 // dropping that z and all above it for this view.  Called rarely (symmetric
 // geometries); kept out of line so the hot loop keeps its registers.
 __device__ __noinline__ int chord_end_z(const ConeGeom &g, int ti, int si, double sb, double cb, int zlo, int zhi,
-                                        bool tie_ts, float ztie, bool tz1, float zc1, bool tz2, float zc2) {
+                                        bool tie_ts, float ztie, float mmax, bool tz1, float zc1, bool tz2, float zc2) {
     const float rz = (float)g.res[2];
+    const float hz = 0.5f * rz;
     const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);
     int zab = 0x7fffffff;
+    // A face crossing lies |iz| * h_a / |d_a| off the voxel centre in z.  Where
+    // that stays below hz (10% margin) at every z of the column, the z parts of
+    // the t and s face tests pass everywhere and their z-independent in-plane
+    // parts decide every z at once; near the diagonal views this replaces a
+    // per-z FP64 replay of the whole column.
+    const float izc = fmaxf(fabsf(fmaf((float)max(zlo, 0), rz, x_base)), fabsf(fmaf((float)min(zhi, g.nz - 1), rz, x_base)));
+    if (tie_ts && izc * mmax < 0.9f * hz && chord_side_found(g, ti, si, sb, cb)) tie_ts = false;
     if (tie_ts) {
         // t/s faces limit the chord where |iz| <= ztie: check those z in order
         for (int z = max(zlo, 0); z <= min(zhi, g.nz - 1); ++z) {
@@ -150,9 +181,13 @@ __device__ __noinline__ int chord_end_z(const ConeGeom &g, int ti, int si, doubl
     return min(zhi, zab - 1);
 }
 
+// Views [v0, v0 + nv) of the scan, whose quads Q holds (Q[0] = view v0).
+// Each voxel's sum b = (sum over these views) + prev (when prev is given) is
+// written to out, or with UPDATE folded into out = vol as
+// clamp(vol + lambda * b / (colsum + eps), lo, hi).
 template <int WMODE, bool UPDATE>
 __global__ void __launch_bounds__(BP_BX * BP_BY, CT_BP_MINB)
-cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict__ vol,
+cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, const float *prev, float *out,
                const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
     // the row table (x - q(xi[x]), q(xi[x+1]) - x) of ConeGeom::xtab
     extern __shared__ float2 xtab[];
@@ -192,7 +227,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
 #pragma unroll
     for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
 
-    for (int v = 0; v < g.nb; ++v) {
+    for (int v = v0; v < v0 + nv; ++v) {
         const double2 tr = g.trig[v];
         const float sb = (float)tr.x, cb = (float)tr.y;
         // detector coordinates of the column in float-float: the reference's
@@ -222,7 +257,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         const float pa = __ldg(g.P + p1), pb = __ldg(g.P + p1 + 1);
         const float wq1 = fabsf(__fadd_rn(__fsub_rn(P2.hi, pa), P2.lo)) * ipint;   // weight of column p1+1
         const float wq0 = fabsf(__fsub_rn(__fsub_rn(pb, P2.hi), P2.lo)) * ipint;   // weight of column p1
-        const float4 *Qv = Q + (long long)v * vstride + p1;
+        const float4 *Qv = Q + (long long)(v - v0) * vstride + p1;
         // row quotient q(z) = |xi(z) - xi[0]| / XigamaInt, affine in z, as 64-bit
         // fixed point (32 fraction bits): floor and weights follow the
         // reference's FP64 values except within ~1e-8 of a row boundary
@@ -254,7 +289,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
                 tz2 = fabsf(zc2 - rintf(zc2)) < 1e-3f;
             }
             if (tie_ts || tz1 || tz2)
-                zend = chord_end_z(g, ti, si, tr.x, tr.y, zlo, zhi, tie_ts, hz / mts, tz1, zc1, tz2, zc2);
+                zend = chord_end_z(g, ti, si, tr.x, tr.y, zlo, zhi, tie_ts, hz / mts, fmaxf(mt, ms), tz1, zc1, tz2,
+                                   zc2);
         } else {
             wv = lr * lr * g.bint;
         }
@@ -309,11 +345,12 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
         const int z = z0 + k;
         if (z < g.nz) {
             const long long o = ((long long)z * g.ns + si) * g.nt + ti;
+            const float b = prev ? acc[k] + prev[o] : acc[k];
             if (UPDATE) {
-                const float x = vol[o] + lambda * acc[k] / (colsum[o] + eps);
-                vol[o] = fminf(fmaxf(x, lo), hi);
+                const float x = out[o] + lambda * b / (colsum[o] + eps);
+                out[o] = fminf(fmaxf(x, lo), hi);
             } else {
-                vol[o] = acc[k];
+                out[o] = b;
             }
         }
     }
@@ -321,26 +358,27 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, float *__restrict
 
 }  // namespace
 
-size_t cone_quads_bytes(const ConeGeom &g) { return sizeof(float4) * (size_t)g.nb * g.nx * g.np; }
+size_t cone_quads_bytes(const ConeGeom &g, int nviews) { return sizeof(float4) * (size_t)nviews * g.nx * g.np; }
 
-int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, cudaStream_t st) {
-    const long long n = (long long)g.nb * g.nx * g.np;
+int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, int v0, int nv, cudaStream_t st) {
+    const long long n = (long long)nv * g.nx * g.np;
     int blocks = (int)std::min<long long>((n + 255) / 256, (long long)sm_count() * 16);
-    pack_quads_kernel<<<blocks, 256, 0, st>>>(R, Q, g.nb, g.nx, g.np);
+    pack_quads_kernel<<<blocks, 256, 0, st>>>(R + (long long)v0 * g.nx * g.np, Q, nv, g.nx, g.np);
     CT_LAUNCH_CHECK("pack_quads_kernel");
     return CT_OK;
 }
 
 // weighting: 0 chord, 1 FDK (off-detector adds 0), 2 FDK sticky
-int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting, const float *colsum,
-                   float eps, float lambda, float lo, float hi, bool update, cudaStream_t st) {
+int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const float *prev, float *out, int weighting,
+                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st) {
     CT_REQUIRE(g.np >= 2 && g.nx >= 2, "cone_bp: detector needs at least 2x2 samples");
+    CT_REQUIRE(v0 >= 0 && nv > 0 && v0 + nv <= g.nb, "cone_bp: view range out of bounds");
     dim3 block(BP_BX, BP_BY);
     dim3 grid((g.nt + BP_BX - 1) / BP_BX, (g.ns + BP_BY - 1) / BP_BY, (g.nz + BP_ZC - 1) / BP_ZC);
     const size_t smem = sizeof(float2) * (size_t)g.nx;
     CT_REQUIRE(smem <= 48 * 1024, "cone_bp: at most 6144 detector rows");
 #define CT_BP_CASE(W, U)                                                                     \
-    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, vol, colsum, eps, lambda, lo, hi)
+    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, v0, nv, prev, out, colsum, eps, lambda, lo, hi)
     if (update) {
         if (weighting == W_CHORD) CT_BP_CASE(W_CHORD, true);
         else if (weighting == W_FDK_ZERO) CT_BP_CASE(W_FDK_ZERO, true);

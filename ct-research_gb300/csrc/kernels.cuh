@@ -74,10 +74,14 @@ int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const flo
                       float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_double, const float *b,
                      const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
-size_t cone_quads_bytes(const ConeGeom &g);
-int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, cudaStream_t st);
-int cone_bp_launch(const ConeGeom &g, const float4 *Q, float *vol, int weighting, const float *colsum,
-                   float eps, float lambda, float lo, float hi, bool update, cudaStream_t st);
+// Backprojection in view chunks: the quads of views [v0, v0 + nv) of the full
+// sinogram R are packed into Q, then backprojected; each voxel's chunk sum plus
+// prev (optional) goes to out, or, with update, into out = vol as
+// clamp(vol + lambda * sum / (colsum + eps), lo, hi).
+size_t cone_quads_bytes(const ConeGeom &g, int nviews);
+int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, int v0, int nv, cudaStream_t st);
+int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const float *prev, float *out, int weighting,
+                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st);
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st);
 int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);

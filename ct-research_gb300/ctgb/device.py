@@ -113,6 +113,20 @@ class ConePlan:
                   len(geom.xi), float(geom.D))
         _lib.call("ct_cone_plan_set_fdk_mode", self._h, int(fdk_filter), int(fdk_bp))
         self._norms = None
+        self.bp_chunk = 0
+
+    def set_bp_chunk(self, views: int):
+        """Views per backprojection chunk (0: all views in one pass, the default)."""
+        _lib.call("ct_cone_plan_set_bp_chunk", self._h, int(views))
+        self.bp_chunk = int(views)
+        return self
+
+    def launches_per_pair(self) -> int:
+        """Kernels of one fp + bp: layout transpose, walk, grazing re-walk, and
+        per backprojection chunk the quad packing and the backprojection."""
+        nb = len(self.geom.beta)
+        chunk = min(self.bp_chunk, nb) if self.bp_chunk > 0 else nb
+        return 3 + 2 * -(-nb // chunk)
 
     def set_filter(self, kind="shepp-logan", window: int = 0, short_scan: bool = False):
         """FDK filter stage: ramp taps, Hamming smoothing window length (0 =

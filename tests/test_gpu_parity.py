@@ -293,3 +293,26 @@ def test_bad_arguments_raise():
     out = ops.ProjectionCone_3D(np.zeros(8 ** 3, np.float32), 8, 8, 8, [10, 10, 10], [0.1, 0.2], [-1, 0, 1],
                                 [-1, 1], 5.0, on_error="zeros")
     assert out.shape == (12,) and not out.any()
+
+
+def test_bp_view_chunks_match_one_pass(oracle, torch_cuda):
+    """Backprojection in chunks of views: chunk sums are added in float, so the
+    result differs from one pass only by rounding."""
+    from ctgb.device import ConePlan
+    torch = torch_cuda
+    geom, vol = _random_cone(13, nb=30)
+    R = torch.rand(geom.sino_shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
+    one = ConePlan(geom)
+    many = ConePlan(geom).set_bp_chunk(7)                # 5 chunks, the last one shorter
+    a, b = one.bp(R), many.bp(R)
+    assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) <= 1e-6
+    ref = oracle.cone_bp(R.cpu().numpy(), geom.beta, geom.P, geom.xi, geom.size, geom.D, geom.vol_shape)
+    assert rel_l2(b.cpu().numpy(), ref) <= TOL
+    colsum = one.bp(torch.ones_like(R))
+    x0 = torch.from_numpy(vol).cuda()
+    x1, x2 = x0.clone(), x0.clone()
+    one.bp_update(R, colsum, x1, lam=0.7, eps=1e-3, lo=0.0, hi=1.0)
+    many.bp_update(R, colsum, x2, lam=0.7, eps=1e-3, lo=0.0, hi=1.0)
+    assert rel_l2(x2.cpu().numpy(), x1.cpu().numpy()) <= 1e-6
+    f1, f2 = one.fdk(R), many.fdk(R)
+    assert rel_l2(f2.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
