@@ -110,48 +110,77 @@ static __device__ __noinline__ float fan_chord_fp64(const FanGeom &g, int ti, in
 __device__ __forceinline__ bool ff_ge(ff a, float b) { return a.hi > b || (a.hi == b && a.lo >= 0.0f); }
 __device__ __forceinline__ bool ff_lt(ff a, float b) { return a.hi < b || (a.hi == b && a.lo < 0.0f); }
 
+// The reference's detector coordinate P / U of pixel (ti, si) in one view in
+// float-float (ffloat.cuh), for the pixel-views where the FP32 value lies near
+// a decision boundary.  One division, by a reciprocal and a float-float
+// correction.
+static __device__ __noinline__ ff fan_pd_ff(const FanGeom &g, int ti, int si, float sb, float cb, int wmode) {
+    const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
+    const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const ff P2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
+    if (wmode == BP2_FBPPAR) return P2;
+    const ff R2 = ff_from(g.D);
+    const ff den = ff_sub(R2, ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb)));   // Rscan - S
+    const ff num = ff_mul(P2, R2);                                             // P / ((Rscan - S) / Rscan)
+    const float r = __frcp_rn(den.hi);
+    const float q1 = __fmul_rn(num.hi, r);
+    const ff rem = ff_sub(num, ff_mul_f(den, q1));
+    return ff_fast2sum(q1, __fmul_rn(rem.hi, r));
+}
+
 // Sum over all views for pixel i (t fastest) with the weighting WMODE.
-// The detector coordinate follows the reference's FP64 P / U in float-float
-// (ffloat.cuh): the bin is floor(|Pd - P0| / PInt) with PInt the spacing of
-// the first two samples and weights |Pd - P[i]| / PInt from the actual sample
-// values, a discontinuous rule (float samples drift from the implied grid, by
-// ~1e-3 mm over 1024 bins) that FP32 coordinates do not reproduce at large
-// detectors.
+// The bin is the reference's floor(|Pd - P0| / PInt), PInt the spacing of the
+// first two samples, with weights |Pd - P[i]| / PInt from the actual sample
+// values: a discontinuous rule (float samples drift from the implied grid, by
+// ~1e-3 mm over 1024 bins) that an FP32 Pd reproduces except near a bin or
+// range boundary.  There (about 1e-3 of the pixel-views) Pd is recomputed in
+// float-float, as the reference's FP64 value.
 template <int WMODE>
 __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__restrict__ R, int i) {
     const int ti = i % g.nt, si = i / g.nt;
-    const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
-    const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
-    const ff Rs2 = ff_from(g.D), p02 = {g.p0, 0.0f};
-    const ff ipint2 = ff_from(1.0 / (double)g.pint);
+    const float it = (float)((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
+    const float is = (float)((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
     const float Rs = (float)g.D;
     const float ipint = 1.0f / g.pint;
     // pixel edges in world coordinates (BackprojectionFan2D.cu:82)
-    const float tlo = (float)(ti * g.res[0]), thi_ = (float)((ti + 1) * g.res[0]);
-    const float slo = (float)(si * g.res[1]), shi_ = (float)((si + 1) * g.res[1]);
+    const float tlo = (float)(ti * g.res[0]), slo = (float)(si * g.res[1]);
     const float ct_ = (float)(0.5 * g.size[0]), cs_ = (float)(0.5 * g.size[1]);
-    // FP32 rounding of the edge tests is ~1e-5 of the scan's extent
-    const float tie_m = 4e-6f * (Rs + (float)(g.size[0] + g.size[1]));
+    // pixel centre and half sizes, in world coordinates
+    const float pct = (float)((ti + 0.5) * g.res[0]), pcs = (float)((si + 0.5) * g.res[1]);
+    const float ht = (float)(0.5 * g.res[0]), hs = (float)(0.5 * g.res[1]);
+    // FP32 error of Pd is a few ulp of the scan's extent (~3e-4 bins at 1024 bins of
+    // 0.78 mm): within 3x that of a bin or range boundary Pd is recomputed
+    const float near_m = 6e-7f * (Rs + (float)(g.size[0] + g.size[1])) * ipint;
     float acc = 0.0f;
     for (int v = 0; v < g.nb; ++v) {
         const float2 tr = g.trig_f[v];
         const float sb = tr.x, cb = tr.y;
-        const ff P2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
-        ff Pd2 = P2;
-        float u = 1.0f;
+        const float P = fmaf(it, cb, is * sb);
+        float Pd = P, u = 1.0f;
         if (WMODE != BP2_FBPPAR) {
-            const ff S2 = ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb));
-            const ff u2 = ff_div(ff_sub(Rs2, S2), Rs2);
-            Pd2 = ff_div(P2, u2);
-            u = u2.hi;
+            const float S = fmaf(is, cb, -it * sb);
+            u = (Rs - S) / Rs;
+            Pd = P / u;
         }
-        const float Pd = Pd2.hi;
+        float Plo = 0.0f;   // low part of Pd where it is recomputed in float-float
+        const float qf = fabsf(Pd - g.p0) * ipint;
+        const bool near = fabsf(qf - rintf(qf)) < near_m || fabsf(Pd - g.minp) * ipint < near_m ||
+                          fabsf(Pd - g.maxp) * ipint < near_m;
+        if (near) {
+            const ff Pd2 = fan_pd_ff(g, ti, si, sb, cb, WMODE);
+            Pd = Pd2.hi;
+            Plo = Pd2.lo;
+        }
+        const ff Pd2 = {Pd, Plo};
         float val = 0.0f;
         if (ff_ge(Pd2, g.minp) && ff_lt(Pd2, g.maxp)) {
-            const int p1 = min(max(ff_floor(ff_mul(ff_abs(ff_sub(Pd2, p02)), ipint2)), 0), g.np - 2);
+            // far from a bin boundary the FP32 quotient has the reference's floor
+            int p1 = near ? ff_floor(ff_mul(ff_abs(ff_sub(Pd2, ff{g.p0, 0.0f})), ff_from(1.0 / (double)g.pint)))
+                          : (int)qf;
+            p1 = min(max(p1, 0), g.np - 2);
             const float pa = __ldg(g.Pf + p1), pb = __ldg(g.Pf + p1 + 1);
-            const float w1 = fabsf(__fadd_rn(__fsub_rn(Pd, pa), Pd2.lo)) * ipint;
-            const float w0 = fabsf(__fsub_rn(__fsub_rn(pb, Pd), Pd2.lo)) * ipint;
+            const float w1 = fabsf(__fadd_rn(__fsub_rn(Pd, pa), Plo)) * ipint;
+            const float w0 = fabsf(__fsub_rn(__fsub_rn(pb, Pd), Plo)) * ipint;
             const float *Rv = R + (long long)v * g.np + p1;
             val = fmaf(w0, __ldg(Rv), w1 * __ldg(Rv + 1));
         }
@@ -160,32 +189,39 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
             const float ex0 = fmaf(Pd, cb, Rs * sb), ey0 = fmaf(Pd, sb, -Rs * cb);
             const float inv = rsqrtf(fmaf(ex0, ex0, ey0 * ey0));
             const float ex = ex0 * inv, ey = ey0 * inv;
-            const float st = ct_ - Rs * sb, ss = cs_ + Rs * cb;
+            const float st = fmaf(-Rs, sb, ct_), ss = fmaf(Rs, cb, cs_);
             const float a_end = 2.0f * Rs;
             float w;
-            const float at = (tlo - st) / ex;
-            const float s_at = fmaf(at, ey, ss);
-            bool tie = fabsf(s_at) < tie_m || fabsf(s_at - shi_) < tie_m;
+            // The line passes through the pixel centre, so its crossing with the low t
+            // edge lies ds_t = -ht ey / ex from the centre in s, and with the low s edge
+            // dt_s = -hs ex / ey in t.  The reference's tests s in [0, s_high] and t in
+            // [0, t_high] are decided on these small offsets, whose FP32 error is ~1e-7 of
+            // their size; within 1e-5 of a bound the FP64 construction decides.
+            const float ds_t = -ht * ey / ex;
+            const float c1 = pcs + ds_t, c2 = hs - ds_t;           // s_at >= 0, s_at <= s_high
+            bool tie = fabsf(c1) < 1e-5f * (pcs + fabsf(ds_t)) || fabsf(c2) < 1e-5f * (hs + fabsf(ds_t));
             bool none = false;
-            float a = at;
-            if (!(s_at >= 0.0f && s_at <= shi_)) {
-                const float as = (slo - ss) / ey;
-                const float t_as = fmaf(as, ex, st);
-                tie = tie || fabsf(t_as) < tie_m || fabsf(t_as - thi_) < tie_m;
-                a = as;
-                none = !(t_as >= 0.0f && t_as <= thi_);
+            float a = (tlo - st) / ex;
+            if (!(c1 >= 0.0f && c2 >= 0.0f)) {
+                const float dt_s = -hs * ex / ey;
+                const float d1 = pct + dt_s, d2 = ht - dt_s;       // t_as >= 0, t_as <= t_high
+                tie = tie || fabsf(d1) < 1e-5f * (pct + fabsf(dt_s)) || fabsf(d2) < 1e-5f * (ht + fabsf(dt_s));
+                a = (slo - ss) / ey;
+                none = !(d1 >= 0.0f && d2 >= 0.0f);
             }
             if (tie) {
-                w = fan_chord_fp64(g, ti, si, (double)sb, (double)cb, (double)Pd + (double)Pd2.lo);
+                // the FP64 construction needs the reference's P / U, not the FP32 one
+                const ff pe = near ? Pd2 : fan_pd_ff(g, ti, si, sb, cb, WMODE);
+                w = fan_chord_fp64(g, ti, si, (double)sb, (double)cb, (double)pe.hi + (double)pe.lo);
             } else {
                 if (none) continue;
                 w = 2.0f * fabsf(a_end - a);
             }
             acc = fmaf(val, w, acc);
         } else if (WMODE == BP2_FBPFAN) {
-            acc += val / (u * u) * g.bint;
+            acc = fmaf(val / (u * u), g.bint, acc);
         } else {
-            acc += val * g.bint;
+            acc = fmaf(val, g.bint, acc);
         }
     }
     return acc;
