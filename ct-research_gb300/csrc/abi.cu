@@ -334,9 +334,10 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     // (detector columns closer to t: |cos b| >= |sin b|, as cone_fp_kernel
     // picks) first, then those that read the [z][t][s] copy
     std::vector<int> vo;
-    for (int pass = 0; pass < 2; ++pass)
-        for (int v = 0; v < nb; ++v)
-            if ((std::fabs(tr[v].y) >= std::fabs(tr[v].x)) == (pass == 0)) vo.push_back(v);
+    for (int c0 = 0; c0 < nb; c0 += kFpViewChunk)
+        for (int pass = 0; pass < 2; ++pass)
+            for (int v = c0; v < std::min(nb, c0 + kFpViewChunk); ++v)
+                if ((std::fabs(tr[v].y) >= std::fabs(tr[v].x)) == (pass == 0)) vo.push_back(v);
     if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->vsrc, vs.data(), nb)) || (s = upload(pl->P, P, np)) ||
         (s = upload(pl->xi, xi, nx)) || (s = upload(pl->xtab, xt.data(), xt.size())) ||
         (s = upload(pl->vorder, vo.data(), vo.size()))) {
@@ -805,11 +806,57 @@ std::mutex g_dropin_mutex;
 struct DropinState {
     ct_cone_plan *cone = nullptr;
     DevBuf vol, proj;
+    // streams and events of the overlapped path (pinned host buffers)
+    int dev = -1;
+    cudaStream_t cs = nullptr, xs = nullptr;   // kernels, and the copies that overlap them
+    std::vector<cudaEvent_t> ev;
 };
 DropinState &dropin() {
     static DropinState st;
     return st;
 }
+
+void dropin_streams_release(DropinState &st) {
+    for (cudaEvent_t e : st.ev) cudaEventDestroy(e);
+    st.ev.clear();
+    if (st.cs) cudaStreamDestroy(st.cs);
+    if (st.xs) cudaStreamDestroy(st.xs);
+    st.cs = st.xs = nullptr;
+    st.dev = -1;
+}
+
+// The two streams and nev events of the overlapped path on the current device.
+int dropin_streams(DropinState &st, int nev) {
+    int dev = 0;
+    CT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (st.cs && st.dev != dev) dropin_streams_release(st);
+    if (!st.cs) {
+        CT_CUDA(cudaStreamCreateWithFlags(&st.cs, cudaStreamNonBlocking), "drop-in stream");
+        CT_CUDA(cudaStreamCreateWithFlags(&st.xs, cudaStreamNonBlocking), "drop-in copy stream");
+        st.dev = dev;
+    }
+    while ((int)st.ev.size() < nev) {
+        cudaEvent_t e;
+        CT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "drop-in event");
+        st.ev.push_back(e);
+    }
+    return CT_OK;
+}
+
+// Page-locked (or registered) host memory: copies from it run asynchronously.
+bool host_pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Views per chunk of the overlapped drop-in path: the forward projection of a
+// chunk overlaps the copy-out of the previous one, and the copy-in of a chunk
+// the backprojection of the previous one.
+constexpr int kDropinChunk = kFpViewChunk;
 
 // Reuse the cached cone plan when the geometry is unchanged.
 int cached_cone_plan(ct_cone_plan **out, int nt, int ns, int nz, const double *Size, const float *beta, int nb,
@@ -844,6 +891,7 @@ int ct_dropin_release(void) {
         st.cone = nullptr;
         st.vol.release();
         st.proj.release();
+        dropin_streams_release(st);
     }
     iterfdk_release_cache();
     fdkui_release_cache();
@@ -874,9 +922,35 @@ int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaS
     DropinState &st = dropin();
     const size_t nv = (size_t)t_length * s_length * z_length, npj = (size_t)LBeta * LP * LXigama;
     if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;
-    CT_CUDA(cudaMemcpy(st.vol.ptr, Pic, nv * sizeof(float), cudaMemcpyHostToDevice), "H2D volume");
-    if ((s = ct_cone_fp(pl, st.vol.as<float>(), st.proj.as<float>(), nullptr))) return s;
-    CT_CUDA(cudaMemcpy(Projection, st.proj.ptr, npj * sizeof(float), cudaMemcpyDeviceToHost), "D2H projection");
+    if (LBeta <= kDropinChunk || !host_pinned(Pic) || !host_pinned(Projection)) {
+        CT_CUDA(cudaMemcpy(st.vol.ptr, Pic, nv * sizeof(float), cudaMemcpyHostToDevice), "H2D volume");
+        if ((s = ct_cone_fp(pl, st.vol.as<float>(), st.proj.as<float>(), nullptr))) return s;
+        CT_CUDA(cudaMemcpy(Projection, st.proj.ptr, npj * sizeof(float), cudaMemcpyDeviceToHost), "D2H projection");
+        return CT_OK;
+    }
+    // pinned buffers: project view chunks and copy each chunk out while the next is projected
+    const int nchunks = (LBeta + kDropinChunk - 1) / kDropinChunk;
+    if ((s = dropin_streams(st, nchunks))) return s;
+    CT_CUDA(cudaMemcpyAsync(st.vol.ptr, Pic, nv * sizeof(float), cudaMemcpyHostToDevice, st.cs), "H2D volume");
+    GrazeList gl;
+    const float *volS, *volT;
+    if ((s = graze_list(pl->graze, gl, cone_rays(pl->g), st.cs)) ||
+        (s = fp_volumes(pl, st.vol.as<float>(), &volS, &volT, st.cs)))
+        return s;
+    const size_t per_view = (size_t)LP * LXigama;
+    for (int c = 0; c < nchunks; ++c) {
+        const int v0 = c * kDropinChunk, n = std::min(kDropinChunk, LBeta - v0);
+        if ((s = cone_fp_launch(pl->g, volS, volT, st.vol.as<float>(), st.proj.as<float>(), nullptr, nullptr, 0.0f,
+                                nullptr, 0, gl, st.cs, v0, n)))
+            return s;
+        CT_CUDA(cudaEventRecord(st.ev[c], st.cs), "event");
+        CT_CUDA(cudaStreamWaitEvent(st.xs, st.ev[c], 0), "event wait");
+        CT_CUDA(cudaMemcpyAsync(Projection + v0 * per_view, st.proj.as<float>() + v0 * per_view,
+                                n * per_view * sizeof(float), cudaMemcpyDeviceToHost, st.xs),
+                "D2H projection");
+    }
+    CT_CUDA(cudaStreamSynchronize(st.xs), "sync");
+    CT_CUDA(cudaStreamSynchronize(st.cs), "sync");
     return CT_OK;
 }
 
@@ -890,6 +964,33 @@ static int cone_bp_dropin(float *Display, const float *R, const float *xi, const
     DropinState &st = dropin();
     const size_t nv = (size_t)nt * ns * nz, npj = (size_t)nb * np * nx;
     if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;
+    if (!fdk && nb > kDropinChunk && np >= 2 && nx >= 2 && host_pinned(R) && host_pinned(Display)) {
+        // pinned buffers: copy view chunks in, each backprojected (and added to the
+        // volume) while the next one arrives
+        const int nchunks = (nb + kDropinChunk - 1) / kDropinChunk;
+        if ((s = dropin_streams(st, nchunks)) || (s = pl->quads.ensure(cone_quads_bytes(pl->g, kDropinChunk))))
+            return s;
+        const size_t per_view = (size_t)np * nx;
+        for (int c = 0; c < nchunks; ++c) {
+            const int v0 = c * kDropinChunk, n = std::min(kDropinChunk, nb - v0);
+            CT_CUDA(cudaMemcpyAsync(st.proj.as<float>() + v0 * per_view, R + v0 * per_view,
+                                    n * per_view * sizeof(float), cudaMemcpyHostToDevice, st.xs),
+                    "H2D projection");
+            CT_CUDA(cudaEventRecord(st.ev[c], st.xs), "event");
+        }
+        for (int c = 0; c < nchunks; ++c) {
+            const int v0 = c * kDropinChunk, n = std::min(kDropinChunk, nb - v0);
+            CT_CUDA(cudaStreamWaitEvent(st.cs, st.ev[c], 0), "event wait");
+            if ((s = cone_pack_quads(pl->g, st.proj.as<float>(), pl->quads.as<float4>(), v0, n, st.cs)) ||
+                (s = cone_bp_launch(pl->g, pl->quads.as<float4>(), v0, n, c == 0 ? nullptr : st.vol.as<float>(),
+                                    st.vol.as<float>(), 0, nullptr, 0.f, 0.f, 0.f, 0.f, false, st.cs)))
+                return s;
+        }
+        CT_CUDA(cudaMemcpyAsync(Display, st.vol.ptr, nv * sizeof(float), cudaMemcpyDeviceToHost, st.cs),
+                "D2H volume");
+        CT_CUDA(cudaStreamSynchronize(st.cs), "sync");
+        return CT_OK;
+    }
     CT_CUDA(cudaMemcpy(st.proj.ptr, R, npj * sizeof(float), cudaMemcpyHostToDevice), "H2D projection");
     s = fdk ? ct_cone_fdk(pl, st.proj.as<float>(), st.vol.as<float>(), nullptr)
             : ct_cone_bp(pl, st.proj.as<float>(), st.vol.as<float>(), nullptr);

@@ -40,16 +40,16 @@ constexpr int FP_BY = 4;    // detector rows per block
 // MODE 2: count segments into *norms (as double).
 template <int MODE>
 __global__ void __launch_bounds__(FP_BX * FP_BY, CT_FP_MINB)
-cone_fp_kernel(const ConeGeom g, const float *__restrict__ vol, const float *__restrict__ volT,
+cone_fp_kernel(const ConeGeom g, int v0, const float *__restrict__ vol, const float *__restrict__ volT,
                float *__restrict__ out, const float *__restrict__ b, const float *__restrict__ rowsum, float eps,
                double *__restrict__ norms, const GrazeList gl) {
     const int p = blockIdx.x * FP_BX + threadIdx.x;
 #if CT_FP_VIEW_INNER
     const int x = blockIdx.z * FP_BY + threadIdx.y;
-    const int v = g.vorder[blockIdx.y];
+    const int v = g.vorder[v0 + blockIdx.y];
 #else
     const int x = blockIdx.y * FP_BY + threadIdx.y;
-    const int v = blockIdx.z;
+    const int v = v0 + blockIdx.z;
 #endif
     const bool active = p < g.np && x < g.nx;
     const int nmax = g.nt * g.ns * g.nz - 1;
@@ -119,22 +119,24 @@ int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStre
 
 int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const float *volU, float *out,
                    const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
-                   cudaStream_t st) {
+                   cudaStream_t st, int v0, int nv) {
+    if (nv <= 0) nv = g.nb - v0;
+    CT_REQUIRE(v0 >= 0 && v0 + nv <= g.nb, "cone_fp: view range out of bounds");
     dim3 block(FP_BX, FP_BY);
 #if CT_FP_VIEW_INNER
-    dim3 grid((g.np + FP_BX - 1) / FP_BX, g.nb, (g.nx + FP_BY - 1) / FP_BY);
+    dim3 grid((g.np + FP_BX - 1) / FP_BX, nv, (g.nx + FP_BY - 1) / FP_BY);
 #else
-    dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, g.nb);
+    dim3 grid((g.np + FP_BX - 1) / FP_BX, (g.nx + FP_BY - 1) / FP_BY, nv);
 #endif
-    CT_REQUIRE(g.nb <= 65535, "cone_fp: at most 65535 views per launch");
+    CT_REQUIRE(nv <= 65535, "cone_fp: at most 65535 views per launch");
     CT_REQUIRE((g.nx + FP_BY - 1) / FP_BY <= 65535, "cone_fp: at most 262140 detector rows");
     if (mode != 2) CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     if (mode == 0)
-        cone_fp_kernel<0><<<grid, block, 0, st>>>(g, vol, volT, out, nullptr, nullptr, 0.0f, nullptr, gl);
+        cone_fp_kernel<0><<<grid, block, 0, st>>>(g, v0, vol, volT, out, nullptr, nullptr, 0.0f, nullptr, gl);
     else if (mode == 1)
-        cone_fp_kernel<1><<<grid, block, 0, st>>>(g, vol, volT, out, b, rowsum, eps, norms, gl);
+        cone_fp_kernel<1><<<grid, block, 0, st>>>(g, v0, vol, volT, out, b, rowsum, eps, norms, gl);
     else
-        cone_fp_kernel<2><<<grid, block, 0, st>>>(g, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0f, norms, gl);
+        cone_fp_kernel<2><<<grid, block, 0, st>>>(g, v0, nullptr, nullptr, nullptr, nullptr, nullptr, 0.0f, norms, gl);
     CT_LAUNCH_CHECK("cone_fp_kernel");
     if (mode != 2) return cone_fixup_launch(g, volU, out, b, rowsum, eps, norms, mode, gl, st);
     return CT_OK;

@@ -32,10 +32,12 @@ struct ConeGeom {
     // the bilinear row weights |xi - xi[x]| / xint and |xi[x+1] - xi| / xint of a
     // point with quotient x + f are then |f + tab.x| and |tab.y - f|.
     const float2 *xtab;
-    // View order of the forward projector's launch: the views whose detector
+    // View order of the forward projector's launch, chunk by chunk of
+    // kFpViewChunk consecutive views: in each chunk the views whose detector
     // columns run closer to t (read from the [z][s][t] volume) first, then those
-    // read from the [z][t][s] copy, each group in scan order, so that the views
-    // sharing a wave of blocks read the same copy of the volume.
+    // read from the [z][t][s] copy, so that the views sharing a wave of blocks
+    // read the same copy of the volume.  A chunk's views are contiguous in the
+    // sinogram: a chunk can be projected and copied out on its own.
     const int *vorder;
 };
 

@@ -65,10 +65,13 @@ __device__ __forceinline__ void graze_push(const GrazeList &gl, unsigned long lo
 // detector rows run closer to the s axis; both point kFpPadSlices slices into
 // zero-padded copies (the walk reads unclamped, see siddon.cuh).  volU is the
 // caller's volume, read by the FP64 re-walk of grazing rays.
+// v0, nv: a range of the launch order ConeGeom::vorder (chunks of kFpViewChunk
+// views, each chunk grouped by volume copy); nv = 0: from v0 to the end.
 constexpr int kFpPadSlices = 4;
+constexpr int kFpViewChunk = 90;
 int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const float *volU, float *out,
                    const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
-                   cudaStream_t st);
+                   cudaStream_t st, int v0 = 0, int nv = 0);
 int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStream_t st);
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
                       float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);

@@ -316,3 +316,42 @@ def test_bp_view_chunks_match_one_pass(oracle, torch_cuda):
     assert rel_l2(x2.cpu().numpy(), x1.cpu().numpy()) <= 1e-6
     f1, f2 = one.fdk(R), many.fdk(R)
     assert rel_l2(f2.cpu().numpy(), f1.cpu().numpy()) <= 1e-6
+
+
+def test_dropin_pinned_overlap_matches_pageable(torch_cuda):
+    """Pinned host buffers take the overlapped drop-in path (view chunks copied
+    out while the next chunk is projected, copied in while the previous one is
+    backprojected).  The forward projection is the same arithmetic per ray, so
+    bit-identical to the pageable path; the backprojection adds chunk sums in
+    float, so it differs from one pass only by rounding."""
+    import ctypes as C
+    from ctgb import _lib
+    torch = torch_cuda
+    geom, vol = _random_cone(17, shape=(24, 28, 32), nb=200, np_=40, nx=24)
+    lib = _lib.lib()
+    res = np.array([geom.size[0] / geom.nt, geom.size[1] / geom.ns, geom.size[2] / geom.nz])
+    size = np.array(geom.size, dtype=np.float64)
+    vp = lambda a: C.c_void_p(a.ctypes.data) if isinstance(a, np.ndarray) else C.c_void_p(a.data_ptr())
+
+    def run(h_vol, h_proj, h_back):
+        _lib.check(lib.ct_ProjectionCone_3D(vp(h_vol), vp(h_proj), vp(geom.beta), vp(geom.P), vp(geom.xi),
+                                            geom.nt, geom.ns, geom.nz, size[0] / 2, size[1] / 2, size[2] / 2,
+                                            len(geom.beta), len(geom.P), len(geom.xi), geom.D, vp(res)),
+                   "ct_ProjectionCone_3D")
+        _lib.check(lib.ct_BackPro(vp(h_back), vp(h_proj), vp(geom.xi), vp(geom.P), vp(geom.beta), geom.D,
+                                  len(geom.beta), len(geom.P), len(geom.xi), vp(size), geom.nt, geom.ns, geom.nz),
+                   "ct_BackPro")
+
+    page = [np.ascontiguousarray(vol, np.float32), np.zeros(geom.sino_shape, np.float32),
+            np.zeros(geom.vol_shape, np.float32)]
+    run(*page)
+    pin = [torch.empty(s, dtype=torch.float32, pin_memory=True) for s in (geom.vol_shape, geom.sino_shape,
+                                                                         geom.vol_shape)]
+    pin[0].copy_(torch.from_numpy(page[0]))
+    for rep in range(2):                           # the second call reuses the streams and events
+        pin[1].fill_(-1.0)
+        pin[2].fill_(-1.0)
+        run(*pin)
+        assert np.array_equal(pin[1].numpy(), page[1])
+        assert rel_l2(pin[2].numpy(), page[2]) <= 1e-6
+    _lib.check(lib.ct_dropin_release(), "ct_dropin_release")
