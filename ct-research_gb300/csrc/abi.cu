@@ -211,7 +211,7 @@ using namespace ct;
 // ---------------------------------------------------------------------------
 struct ct_cone_plan {
     ConeGeom g{};
-    DevBuf trig, vsrc, P, xi, xtab, vorder;
+    DevBuf trig, vsrc, P, xi, xtab, vorder, trigf, vsrcf, Pd, xid;
     DevBuf quads, rcov, G, wtab, norms, volT, volS, pwt, win, scan, bpsum;
     GrazeBuf graze;
     int bp_chunk = 0;   // views per backprojection chunk; 0: all views in one pass
@@ -224,6 +224,7 @@ struct ct_cone_plan {
     double hsize[3] = {0, 0, 0};
     ~ct_cone_plan() {
         trig.release(); vsrc.release(); P.release(); xi.release(); xtab.release(); vorder.release();
+        trigf.release(); vsrcf.release(); Pd.release(); xid.release();
         quads.release(); rcov.release(); G.release(); wtab.release(); norms.release(); graze.release();
         volT.release(); volS.release(); pwt.release(); win.release(); scan.release(); bpsum.release();
     }
@@ -300,6 +301,7 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     g.res[1] = 1.0 * Size[1] / ns;
     g.res[2] = 1.0 * Size[2] / nz;
     for (int a = 0; a < 3; ++a) g.ires[a] = 1.0 / g.res[a];
+    cone_geom_derive(g);
     g.D = D;
     // float-range bookkeeping of BackPro / FDKpro (Backprojection3D.cu:304-311)
     g.pint = np > 1 ? std::fabs(P[1] - P[0]) : 1.0f;
@@ -317,11 +319,17 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     // single-precision overloads (ProjectionCone_3D.cu:26-28)
     std::vector<double2> tr(nb);
     std::vector<ViewSrc> vs(nb);
+    std::vector<float2> trf(nb);
+    std::vector<float4> vsf(nb);
     for (int v = 0; v < nb; ++v) {
-        const double sb = (double)sinf(beta[v]), cb = (double)cosf(beta[v]);
+        const float sf = sinf(beta[v]), cf = cosf(beta[v]);
+        const double sb = (double)sf, cb = (double)cf;
         tr[v] = make_double2(sb, cb);
+        trf[v] = make_float2(sf, cf);
         vs[v] = ViewSrc{Size[0] / 2 - D * sb, Size[1] / 2 + D * cb, D * sb, D * cb};
+        vsf[v] = make_float4((float)vs[v].src_t, (float)vs[v].src_s, (float)vs[v].dsb, (float)vs[v].dcb);
     }
+    const std::vector<double> Pdv(P, P + np), xidv(xi, xi + nx);
     // row table of the backprojectors: (x - q(xi[x]), q(xi[x+1]) - x) with the
     // reference's row quotient q(v) = |v - xi[0]| / XigamaInt in double
     std::vector<float2> xt(std::max(nx - 1, 1));
@@ -340,7 +348,9 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
                 if ((std::fabs(tr[v].y) >= std::fabs(tr[v].x)) == (pass == 0)) vo.push_back(v);
     if ((s = upload(pl->trig, tr.data(), nb)) || (s = upload(pl->vsrc, vs.data(), nb)) || (s = upload(pl->P, P, np)) ||
         (s = upload(pl->xi, xi, nx)) || (s = upload(pl->xtab, xt.data(), xt.size())) ||
-        (s = upload(pl->vorder, vo.data(), vo.size()))) {
+        (s = upload(pl->vorder, vo.data(), vo.size())) || (s = upload(pl->trigf, trf.data(), nb)) ||
+        (s = upload(pl->vsrcf, vsf.data(), nb)) || (s = upload(pl->Pd, Pdv.data(), np)) ||
+        (s = upload(pl->xid, xidv.data(), nx))) {
         delete pl;
         return s;
     }
@@ -348,6 +358,10 @@ int ct_cone_plan_create(ct_cone_plan **out, int nt, int ns, int nz, const double
     g.vorder = pl->vorder.as<int>();
     g.trig = pl->trig.as<double2>();
     g.vsrc = pl->vsrc.as<ViewSrc>();
+    g.trigf = pl->trigf.as<float2>();
+    g.vsrcf = pl->vsrcf.as<float4>();
+    g.Pd = pl->Pd.as<double>();
+    g.xid = pl->xid.as<double>();
     g.P = pl->P.as<float>();
     g.xi = pl->xi.as<float>();
     pl->hb.assign(beta, beta + nb);
@@ -919,6 +933,7 @@ int ct_ProjectionCone_3D(const float *Pic, float *Projection, const float *BetaS
         pl->g.res[a] = resolution[a];
         pl->g.ires[a] = 1.0 / resolution[a];
     }
+    cone_geom_derive(pl->g);
     DropinState &st = dropin();
     const size_t nv = (size_t)t_length * s_length * z_length, npj = (size_t)LBeta * LP * LXigama;
     if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;

@@ -228,8 +228,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
     for (int k = 0; k < BP_ZC; ++k) acc[k] = 0.0f;
 
     for (int v = v0; v < v0 + nv; ++v) {
-        const double2 tr = g.trig[v];
-        const float sb = (float)tr.x, cb = (float)tr.y;
+        const float2 tr = g.trigf[v];   // float (sin, cos): no FP64 conversion in the loop
+        const float sb = tr.x, cb = tr.y;
         // detector coordinates of the column in float-float: the reference's
         // FP64 dect_t, dect_s, LengthRatio = D / (D - dect_s) and P = dect_t * LR
         // (Backprojection3D.cu:28-37)
@@ -248,7 +248,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         // FP32 rounding is ~3e-5 in z units: re-decide in FP64 near an edge
         const bool near_edge = fabsf(zlo_f - rintf(zlo_f)) < 2.5e-4f || fabsf(zhi_f - rintf(zhi_f)) < 2.5e-4f ||
                                fabsf(P - g.minp) < 2e-4f || fabsf(P - g.maxp) < 2e-4f;
-        if (near_edge) range_fp64(g, ti, si, tr.x, tr.y, pin, zlo, zhi);
+        if (near_edge) range_fp64(g, ti, si, g.trig[v].x, g.trig[v].y, pin, zlo, zhi);
         if (!pin) continue;   // whole column off the detector for this view
         if (WMODE == W_FDK_STICKY && zhi < zlo) continue;
         // detector column floor(|P - P0| / PInt) and weights |P - P[p1]| / PInt,
@@ -289,7 +289,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
                 tz2 = fabsf(zc2 - rintf(zc2)) < 1e-3f;
             }
             if (tie_ts || tz1 || tz2)
-                zend = chord_end_z(g, ti, si, tr.x, tr.y, zlo, zhi, tie_ts, hz / mts, fmaxf(mt, ms), tz1, zc1, tz2,
+                zend = chord_end_z(g, ti, si, g.trig[v].x, g.trig[v].y, zlo, zhi, tie_ts, hz / mts, fmaxf(mt, ms), tz1, zc1, tz2,
                                    zc2);
         } else {
             wv = lr * lr * g.bint;

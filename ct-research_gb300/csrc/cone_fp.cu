@@ -60,8 +60,8 @@ cone_fp_kernel(const ConeGeom g, int v0, const float *__restrict__ vol, const fl
         // detector neighbours in P are offset along (cos b, sin b): read the copy
         // of the volume whose fastest axis is closest to that direction, so the
         // gathers of a warp fall on few sectors
-        const double2 tr = g.trig[v];
-        const bool use_t = volT && fabs(tr.x) > fabs(tr.y);
+        const float2 tr = g.trigf[v];
+        const bool use_t = volT && fabsf(tr.x) > fabsf(tr.y);
         const bool hit = ray_setup(g, v, p, x, use_t, w);
         if (MODE == 2) {
             r2 = hit ? (float)w.nseg : 0.0f;   // exact: counts < 2^19

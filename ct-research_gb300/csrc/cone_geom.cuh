@@ -22,6 +22,17 @@ struct ConeGeom {
     const ViewSrc *vsrc;     // per view source and D sin / D cos, FP64
     const float *P;          // detector column coordinates
     const float *xi;         // detector row coordinates
+    // The same values in the other precision, so that hot loops convert
+    // nothing (a conversion to or from double issues on the FP64 pipe, which
+    // runs at a small fraction of the FP32 rate on this GPU):
+    const float2 *trigf;     // trig exactly (the values are floats widened)
+    const float4 *vsrcf;     // vsrc rounded to float: (src_t, src_s, D sin, D cos)
+    const double *Pd, *xid;  // P and xi widened
+    double ext[3];           // box extent n * res per axis
+    float extf[3];           // ext rounded to float
+    float iresf[3];          // ires rounded to float
+    double srcz;             // source z: size[2] / 2
+    float srczf;
     // detector sampling as the reference derives it (Backprojection3D.cu:304-311)
     float pint, xint, bint;  // |P1-P0|, |xi1-xi0|, |beta1-beta0|
     float minp, maxp, minx, maxx;
@@ -40,5 +51,18 @@ struct ConeGeom {
     // sinogram: a chunk can be projected and copied out on its own.
     const int *vorder;
 };
+
+// The scalar constants derived from the sizes and the voxel pitch (ext, extf,
+// iresf, srcz, srczf); call again after changing res.
+inline void cone_geom_derive(ConeGeom &g) {
+    const int n[3] = {g.nt, g.ns, g.nz};
+    for (int a = 0; a < 3; ++a) {
+        g.ext[a] = n[a] * g.res[a];
+        g.extf[a] = (float)g.ext[a];
+        g.iresf[a] = (float)g.ires[a];
+    }
+    g.srcz = 0.5 * g.size[2];
+    g.srczf = (float)g.srcz;
+}
 
 }  // namespace ct

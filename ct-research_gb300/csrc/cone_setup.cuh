@@ -26,20 +26,29 @@ __device__ __forceinline__ double drcp1(double x) {
 __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x, bool tr_layout, RayWalk &w) {
     const ViewSrc vs = g.vsrc[v];
     const double2 tr = g.trig[v];
+    const float4 vf = g.vsrcf[v];
+    const float2 trf = g.trigf[v];
     const float Pf = g.P[p], Xf = g.xi[x];
-    const double Pd = (double)Pf;
-    const double src[3] = {vs.src_t, vs.src_s, 0.5 * g.size[2]};
-    const double d[3] = {fma(Pd, tr.y, vs.dsb), fma(Pd, tr.x, -vs.dcb), (double)Xf};
+    const double Pd = g.Pd[p];
+    const double src[3] = {vs.src_t, vs.src_s, g.srcz};
+    const double d[3] = {fma(Pd, tr.y, vs.dsb), fma(Pd, tr.x, -vs.dcb), g.xid[x]};
     const int n[3] = {g.nt, g.ns, g.nz};
+    // signs of d from the bits (no FP64 compare): -1, 0 or +1
+    int sg[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const long long b = __double_as_longlong(d[a]);
+        sg[a] = (b << 1) == 0 ? 0 : (b < 0 ? -1 : 1);
+    }
     // FP32 slab test on FP32 inputs: picks the entry and exit faces
-    const float srcf[3] = {(float)vs.src_t, (float)vs.src_s, (float)src[2]};
-    const float df[3] = {fmaf(Pf, (float)tr.y, (float)vs.dsb), fmaf(Pf, (float)tr.x, -(float)vs.dcb), Xf};
+    const float srcf[3] = {vf.x, vf.y, g.srczf};
+    const float df[3] = {fmaf(Pf, trf.y, vf.z), fmaf(Pf, trf.x, -vf.w), Xf};
     float tin[3], tout[3], idf[3];
     int ax_in = -1, ax_out = -1;
     float fin = -3.0e38f, fout = 3.0e38f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const float hi = (float)(n[a] * g.res[a]);
+        const float hi = g.extf[a];
         idf[a] = __frcp_rn(df[a]);
         if (df[a] != 0.0f) {
             const float t0 = (0.0f - srcf[a]) * idf[a], t1 = (hi - srcf[a]) * idf[a];
@@ -61,13 +70,13 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
     const int ax_in32 = ax_in, ax_out32 = ax_out;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        if (d[a] == 0.0) continue;
+        if (sg[a] == 0) continue;
         const bool cand_in = (a == ax_in32) || (tin[a] > -3.0e38f && fabsf(tin[a] - fin) <= 1e-5f * fabsf(fin));
         const bool cand_out = (a == ax_out32) || (tout[a] < 3.0e38f && fabsf(tout[a] - fout) <= 1e-5f * fabsf(fout));
         if (!(cand_in || cand_out)) continue;
         const double inv = drcp1(d[a]);
-        const double hi = n[a] * g.res[a];
-        const bool pos = d[a] > 0.0;
+        const double hi = g.ext[a];
+        const bool pos = sg[a] > 0;
         // a line going up enters at 0 and leaves at hi; going down the reverse
         if (cand_in) {
             const double t = ((pos ? 0.0 : hi) - src[a]) * inv;
@@ -80,16 +89,15 @@ __device__ __forceinline__ bool ray_setup(const ConeGeom &g, int v, int p, int x
     }
     if (!(a_out > a_in)) return false;
     const float L = (float)(a_out - a_in);
-    int vs0[3], cnt[3], sg[3];
+    int vs0[3], cnt[3];
     float a0[3], da[3];
     bool grazing = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        sg[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
         // entry coordinate in voxel units: exact on the entry face, FP64 elsewhere
         const double gin = (a == ax_in) ? (sg[a] > 0 ? 0.0 : (double)n[a]) : fma(a_in, d[a], src[a]) * g.ires[a];
         const float ginf = (float)gin;
-        const float gstep = df[a] * (float)g.ires[a];               // voxel units per parameter unit
+        const float gstep = df[a] * g.iresf[a];               // voxel units per parameter unit
         const float stepf = fabsf(__frcp_rn(gstep));                // parameter per plane
         const float gout = fmaf(L, gstep, ginf);                    // exit coordinate, FP32
         int s0 = (a == ax_in) ? (sg[a] > 0 ? 0 : n[a] - 1) : (int)floor(gin);
