@@ -318,14 +318,20 @@ def run_ours(args):
 
     d_red = torch.empty(geom.vol_shape, dtype=torch.float32, device=dev) if sharded else None
 
+    call_ms = {"fp": [], "bp": []}
+
     def e2e_step():
+        t0 = time.perf_counter()
         _lib.check(lib.ct_ProjectionCone_3D(vp(h_vol), vp(h_proj), vp(geom.beta), vp(geom.P), vp(geom.xi),
                                             geom.nt, geom.ns, geom.nz, size[0] / 2, size[1] / 2, size[2] / 2,
                                             len(geom.beta), len(geom.P), len(geom.xi), geom.D, vp(res)),
                    "ct_ProjectionCone_3D")
+        t1 = time.perf_counter()
         _lib.check(lib.ct_BackPro(vp(h_back), vp(h_proj), vp(geom.xi), vp(geom.P), vp(geom.beta), geom.D,
                                   len(geom.beta), len(geom.P), len(geom.xi), vp(size), geom.nt, geom.ns, geom.nz),
                    "ct_BackPro")
+        call_ms["fp"].append((t1 - t0) * 1e3)
+        call_ms["bp"].append((time.perf_counter() - t1) * 1e3)
         if sharded:
             # the partial volumes of the ranks' views summed into every rank's host volume
             d_red.copy_(h_back, non_blocking=True)
@@ -349,7 +355,8 @@ def run_ours(args):
     e2e = {"value": job_rays / t_e2e / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": int(h_vol.numel() * 4 + h_proj.numel() * 4 + (h_back.numel() * 4 if sharded else 0)),
            "d2h_bytes_per_step": int(h_proj.numel() * 4 + h_back.numel() * 4 * (2 if sharded else 1)),
-           "ms_per_step": t_e2e * 1e3}
+           "ms_per_step": t_e2e * 1e3,
+           "ms_per_call_median": {k: float(np.median(v[1:])) if len(v) > 1 else None for k, v in call_ms.items()}}
 
     if rank != 0:
         if dist:
@@ -477,6 +484,7 @@ def run_batched2d(args):
     line = {"metric": "batched 2D fan SIRT: GRay/s of FP+BP iterations", "value": rays * iters / t / 1e9,
             "unit": "GRay/s", "ms_per_launch": t * 1e3, "iterations": iters, "slices": len(geoms),
             "rays_per_iteration": rays, "pixels": batch.n_img, "blocks": tune["blocks"],
+            "grazing_rays_per_projection": batch.grazing_rays(),
             "graph_vs_kernels": {"ms_per_iteration_in_graph": per_it, "ms_operators_alone": alone,
                                  "gap_fraction": (per_it - sum(alone.values())) / per_it},
             "residual_first_last_median": [float(np.median(hist[0])), float(np.median(hist[-1]))],

@@ -43,8 +43,15 @@ namespace {
 #ifndef CT_BP_ZC
 #define CT_BP_ZC 32
 #endif
+// Blocks per SM the register allocation aims at.  Chord weighting: 4 (128
+// registers, a few bytes spilled on the out-of-line tie paths) measured 71.8 ms
+// at 512^3 / 360 views against 73.0 ms at 3 (168 registers) and 85.7 ms at 2.
+// FDK weighting at 256^3 / 360 views: 8.08 ms at 3, 8.20 at 4, 12.5 at 5.
 #ifndef CT_BP_MINB
-#define CT_BP_MINB 3
+#define CT_BP_MINB 4
+#endif
+#ifndef CT_BP_MINB_FDK
+#define CT_BP_MINB_FDK 3
 #endif
 constexpr int BP_BX = 32;          // t per block
 constexpr int BP_BY = 4;           // s per block
@@ -186,7 +193,7 @@ __device__ __noinline__ int chord_end_z(const ConeGeom &g, int ti, int si, doubl
 // written to out, or with UPDATE folded into out = vol as
 // clamp(vol + lambda * b / (colsum + eps), lo, hi).
 template <int WMODE, bool UPDATE>
-__global__ void __launch_bounds__(BP_BX * BP_BY, CT_BP_MINB)
+__global__ void __launch_bounds__(BP_BX * BP_BY, WMODE == W_CHORD ? CT_BP_MINB : CT_BP_MINB_FDK)
 cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, const float *prev, float *out,
                const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
     // the row table (x - q(xi[x]), q(xi[x+1]) - x) of ConeGeom::xtab

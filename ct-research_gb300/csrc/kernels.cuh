@@ -61,18 +61,43 @@ __device__ __forceinline__ void graze_push(const GrazeList &gl, unsigned long lo
 }
 #endif
 
+// The in-plane part of the forward projector's walk set-up for one detector
+// column (view v, column p): the rays of a column share the source and the
+// (t, s) part of d, so they enter the volume's (t, s) square at the same
+// parameter and cross the same t and s planes at the same parameters,
+// whatever their row.  Built once per geometry (cone_fp_columns); parameters
+// after a_in are relative to a_in.
+struct __align__(16) FpColumn {
+    double a_in;       // in-plane entry parameter along d (FP64)
+    float a0t, a0s;    // first t / s plane crossing after the entry (+inf: the axis does not move)
+    float dat, das;    // parameter between t / s planes
+    float L;           // in-plane exit
+    float gint, gins;  // entry coordinates along t and s in voxel units
+    float dtf, dsf;    // t and s components of d (FP32)
+    int s0t, s0s;      // entry voxel
+    int cntt, cnts;    // t / s crossings up to the in-plane exit (cntt < 0: the column misses the volume)
+    int flags;         // grazing along a t or s plane; the signs of the t and s components of d
+};
+static_assert(sizeof(FpColumn) == 64, "FpColumn: 64 bytes");
+
 // vol is [z][s][t] and volT the same volume as [z][t][s], read for views whose
 // detector rows run closer to the s axis; both point kFpPadSlices slices into
 // zero-padded copies (the walk reads unclamped, see siddon.cuh).  volU is the
-// caller's volume, read by the FP64 re-walk of grazing rays.
+// caller's volume, read by the FP64 re-walk of grazing rays.  cols is the
+// column table of cone_fp_columns.  mode 0: out = A vol; mode 1:
+// out = (b - A vol) * scale, norms += (|r|^2, |b|^2).
 // v0, nv: a range of the launch order ConeGeom::vorder (chunks of kFpViewChunk
 // views, each chunk grouped by volume copy); nv = 0: from v0 to the end.
 constexpr int kFpPadSlices = 4;
 constexpr int kFpViewChunk = 90;
-int cone_fp_launch(const ConeGeom &g, const float *vol, const float *volT, const float *volU, float *out,
-                   const float *b, const float *rowsum, float eps, double *norms, int mode, const GrazeList &gl,
-                   cudaStream_t st, int v0 = 0, int nv = 0);
+int cone_fp_columns(const ConeGeom &g, FpColumn *cols, cudaStream_t st);
+int cone_fp_launch(const ConeGeom &g, const FpColumn *cols, const float *vol, const float *volT, const float *volU,
+                   float *out, const float *b, const float *rowsum, float eps, double *norms, int mode,
+                   const GrazeList &gl, cudaStream_t st, int v0 = 0, int nv = 0);
 int cone_transpose_ts(const ConeGeom &g, const float *vol, float *volT, cudaStream_t st);
+// Number of walk segments over all rays into *count (as double), with the
+// per-ray set-up the system-matrix export shares (cone_setup.cuh).
+int cone_count_launch(const ConeGeom &g, double *count, cudaStream_t st);
 int cone_fixup_launch(const ConeGeom &g, const float *vol, float *out, const float *b, const float *rowsum,
                       float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_double, const float *b,

@@ -103,15 +103,16 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
 // then advance to the next voxel (ties resolved t, then s, then z).  Every
 // next-crossing parameter is recomputed from its counter with one FMA (an
 // axis that did not advance gets its previous value back exactly), so the
-// step needs no selects.  CLAMP keeps the index inside [0, nmax] for reads
-// from unpadded arrays; without it the caller's array must extend a few
-// slices beyond both ends (a step after the last crossing moves the index by
-// one stride and reads a value weighted by a zero length).
+// step needs no selects.  The segment ends at the next crossing; the caller
+// takes nseg - 1 steps and ends the last segment at the exit parameter L.
+// CLAMP keeps the index inside [0, nmax] for reads from unpadded arrays;
+// without it the caller's array must extend a slice beyond both ends (where
+// rounding lets a crossing of one axis come before the last one of another).
 template <bool CLAMP = true>
 __device__ __forceinline__ void walk_step(RayWalk &w, float &acur, int nmax, float &len, int &vox) {
     const float m12 = fminf(w.n1, w.n2);
     const float m = fminf(w.n0, m12);
-    const float an = fminf(m, w.L);
+    const float an = m;
     len = an - acur;
     acur = an;
     vox = w.idx;
@@ -128,10 +129,15 @@ __device__ __forceinline__ void walk_step(RayWalk &w, float &acur, int nmax, flo
     w.idx = CLAMP ? min(max(nidx, 0), nmax) : nidx;
 }
 
+// Sum of segment length x voxel value along the ray, times |d|: nseg - 1
+// segments end at crossings (four at a time, so four gathers are in flight),
+// the last one at the exit L.
 template <bool CLAMP = true>
 __device__ __forceinline__ float ray_integral(RayWalk &w, const float *__restrict__ vol, int nmax) {
     float acc = 0.0f, acur = 0.0f;
-    for (int it = 0; it < w.nseg; it += 4) {
+    const int ninner = w.nseg - 1;
+    int it = 0;
+    for (; it + 4 <= ninner; it += 4) {
         float l0, l1, l2, l3;
         int i0, i1, i2, i3;
         walk_step<CLAMP>(w, acur, nmax, l0, i0);
@@ -145,6 +151,13 @@ __device__ __forceinline__ float ray_integral(RayWalk &w, const float *__restric
         acc = fmaf(l2, v2, acc);
         acc = fmaf(l3, v3, acc);
     }
+    for (; it < ninner; ++it) {
+        float l;
+        int i;
+        walk_step<CLAMP>(w, acur, nmax, l, i);
+        acc = fmaf(l, __ldg(vol + i), acc);
+    }
+    acc = fmaf(w.L - acur, __ldg(vol + w.idx), acc);
     return acc * w.scale;
 }
 

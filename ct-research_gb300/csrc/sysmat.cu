@@ -33,7 +33,12 @@ __device__ __forceinline__ int csr_walk(RayWalk &w, int nmax, long long base, in
     for (int it = 0; it < w.nseg; ++it) {
         float len;
         int vox;
-        walk_step(w, acur, nmax, len, vox);
+        if (it + 1 < w.nseg) {
+            walk_step(w, acur, nmax, len, vox);
+        } else {   // the last segment ends at the exit
+            len = w.L - acur;
+            vox = w.idx;
+        }
         if (!(len > 0.0f)) continue;
         const float v = len * w.scale;
         if (vox == prev) {

@@ -38,6 +38,7 @@ SIGNATURES = {
     "ct_cone_plan_set_short_scan": (_i, [_vp, _i]),
     "ct_cone_plan_workspace_bytes": (C.c_size_t, [_vp]),
     "ct_cone_plan_set_bp_chunk": (_i, [_vp, _i]),
+    "ct_cone_plan_get_bp_chunk": (_i, [_vp, _vp]),
     "ct_cone_fp": (_i, [_vp, _vp, _vp, _vp]),
     "ct_cone_fp_residual": (_i, [_vp, _vp, _vp, _vp, _f, _vp, _vp, _vp]),
     "ct_cone_bp": (_i, [_vp, _vp, _vp, _vp]),

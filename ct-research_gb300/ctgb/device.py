@@ -116,17 +116,23 @@ class ConePlan:
         self.bp_chunk = 0
 
     def set_bp_chunk(self, views: int):
-        """Views per backprojection chunk (0: all views in one pass, the default)."""
+        """Views per backprojection chunk (0: automatic, the default; >= the
+        view count: one pass)."""
         _lib.call("ct_cone_plan_set_bp_chunk", self._h, int(views))
         self.bp_chunk = int(views)
         return self
+
+    def bp_chunk_views(self) -> int:
+        """Views per backprojection chunk in effect."""
+        n = C.c_int()
+        _lib.call("ct_cone_plan_get_bp_chunk", self._h, C.byref(n))
+        return int(n.value)
 
     def launches_per_pair(self) -> int:
         """Kernels of one fp + bp: layout transpose, walk, grazing re-walk, and
         per backprojection chunk the quad packing and the backprojection."""
         nb = len(self.geom.beta)
-        chunk = min(self.bp_chunk, nb) if self.bp_chunk > 0 else nb
-        return 3 + 2 * -(-nb // chunk)
+        return 3 + 2 * -(-nb // self.bp_chunk_views())
 
     def set_filter(self, kind="shepp-logan", window: int = 0, short_scan: bool = False):
         """FDK filter stage: ramp taps, Hamming smoothing window length (0 =

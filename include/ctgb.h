@@ -172,12 +172,15 @@ int ct_cone_plan_set_short_scan(ct_cone_plan *plan, int enable);
 /* Device bytes of plan-owned workspace (packed sinogram, filter rows). */
 size_t ct_cone_plan_workspace_bytes(const ct_cone_plan *plan);
 /* Views per chunk of the backprojectors (ct_cone_bp, ct_cone_bp_update,
- * ct_cone_fdk_bp and the drop-ins): each chunk's detector data is packed and
- * backprojected on its own and its sums added to the volume; the packed data
- * then needs 16 bytes per detector sample of one chunk instead of the whole
- * scan.  0 (the default): all views in one pass.  Results differ from one pass
- * only by float rounding of the partial sums.  No counterpart in the reference. */
+ * ct_cone_fdk_bp): each chunk's detector data is packed and backprojected on
+ * its own and its sums added to the volume; the packed data needs 16 bytes per
+ * detector sample of one chunk.  0 (the default): automatic, chunks of about
+ * 768 MiB of packed data evened out over the scan (shorter launches keep the
+ * packed views in L2); a value >= the view count: one pass.  Results differ
+ * from one pass only by float rounding of the partial sums.  get returns the
+ * chunk in effect.  No counterpart in the reference. */
 int ct_cone_plan_set_bp_chunk(ct_cone_plan *plan, int views);
+int ct_cone_plan_get_bp_chunk(const ct_cone_plan *plan, int *views);
 
 /* proj[beta][xi][P] = Siddon line integrals of vol.  All pointers are device
  * pointers; work is queued on `stream` (cudaStream_t, 0 = legacy default). */

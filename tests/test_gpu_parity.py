@@ -302,8 +302,9 @@ def test_bp_view_chunks_match_one_pass(oracle, torch_cuda):
     torch = torch_cuda
     geom, vol = _random_cone(13, nb=30)
     R = torch.rand(geom.sino_shape, device="cuda", generator=torch.Generator(device="cuda").manual_seed(3))
-    one = ConePlan(geom)
+    one = ConePlan(geom).set_bp_chunk(len(geom.beta))    # one pass
     many = ConePlan(geom).set_bp_chunk(7)                # 5 chunks, the last one shorter
+    assert one.bp_chunk_views() == 30 and many.bp_chunk_views() == 7
     a, b = one.bp(R), many.bp(R)
     assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) <= 1e-6
     ref = oracle.cone_bp(R.cpu().numpy(), geom.beta, geom.P, geom.xi, geom.size, geom.D, geom.vol_shape)
@@ -355,3 +356,17 @@ def test_dropin_pinned_overlap_matches_pageable(torch_cuda):
         assert np.array_equal(pin[1].numpy(), page[1])
         assert rel_l2(pin[2].numpy(), page[2]) <= 1e-6
     _lib.check(lib.ct_dropin_release(), "ct_dropin_release")
+
+
+def test_bp_automatic_chunk():
+    """Automatic view chunks: about 768 MiB of packed quads per chunk, evened
+    out over the scan (120 views of 768 x 512 at 360 views); small scans in one
+    pass."""
+    from ctgb.device import ConePlan
+    from ctgb.geometry import config_cone_512
+    geom = config_cone_512()
+    assert ConePlan(geom).bp_chunk_views() == 120
+    assert ConePlan(geom.with_views(36)).bp_chunk_views() == 36
+    geom_s, _ = _random_cone(5, nb=30)
+    assert ConePlan(geom_s).bp_chunk_views() == 30
+    assert ConePlan(geom).set_bp_chunk(1000).bp_chunk_views() == 360
