@@ -1019,22 +1019,22 @@ static int cone_bp_dropin(float *Display, const float *R, const float *xi, const
     DropinState &st = dropin();
     const size_t nv = (size_t)nt * ns * nz, npj = (size_t)nb * np * nx;
     if ((s = st.vol.ensure(nv * sizeof(float))) || (s = st.proj.ensure(npj * sizeof(float)))) return s;
-    if (!fdk && nb > kDropinChunk && np >= 2 && nx >= 2 && host_pinned(R) && host_pinned(Display)) {
-        // pinned buffers: copy view chunks in, each backprojected (and added to the
-        // volume) while the next one arrives
-        const int nchunks = (nb + kDropinChunk - 1) / kDropinChunk;
-        if ((s = dropin_streams(st, nchunks)) || (s = pl->quads.ensure(cone_quads_bytes(pl->g, kDropinChunk))))
-            return s;
+    const int bchunk = std::min(cone_bp_chunk_views(pl), kDropinChunk * 2);
+    if (!fdk && nb > bchunk && np >= 2 && nx >= 2 && host_pinned(R) && host_pinned(Display)) {
+        // pinned buffers: copy view chunks (the backprojector's own chunks) in,
+        // each backprojected (and added to the volume) while the next one arrives
+        const int nchunks = (nb + bchunk - 1) / bchunk;
+        if ((s = dropin_streams(st, nchunks)) || (s = pl->quads.ensure(cone_quads_bytes(pl->g, bchunk)))) return s;
         const size_t per_view = (size_t)np * nx;
         for (int c = 0; c < nchunks; ++c) {
-            const int v0 = c * kDropinChunk, n = std::min(kDropinChunk, nb - v0);
+            const int v0 = c * bchunk, n = std::min(bchunk, nb - v0);
             CT_CUDA(cudaMemcpyAsync(st.proj.as<float>() + v0 * per_view, R + v0 * per_view,
                                     n * per_view * sizeof(float), cudaMemcpyHostToDevice, st.xs),
                     "H2D projection");
             CT_CUDA(cudaEventRecord(st.ev[c], st.xs), "event");
         }
         for (int c = 0; c < nchunks; ++c) {
-            const int v0 = c * kDropinChunk, n = std::min(kDropinChunk, nb - v0);
+            const int v0 = c * bchunk, n = std::min(bchunk, nb - v0);
             CT_CUDA(cudaStreamWaitEvent(st.cs, st.ev[c], 0), "event wait");
             if ((s = cone_pack_quads(pl->g, st.proj.as<float>(), pl->quads.as<float4>(), v0, n, st.cs)) ||
                 (s = cone_bp_launch(pl->g, pl->quads.as<float4>(), v0, n, c == 0 ? nullptr : st.vol.as<float>(),
