@@ -356,7 +356,8 @@ def run_ours(args):
            "h2d_bytes_per_step": int(h_vol.numel() * 4 + h_proj.numel() * 4 + (h_back.numel() * 4 if sharded else 0)),
            "d2h_bytes_per_step": int(h_proj.numel() * 4 + h_back.numel() * 4 * (2 if sharded else 1)),
            "ms_per_step": t_e2e * 1e3,
-           "ms_per_call_median": {k: float(np.median(v[1:])) if len(v) > 1 else None for k, v in call_ms.items()}}
+           "ms_per_call_median": {k: float(np.median(v[1:])) if len(v) > 1 else None for k, v in call_ms.items()},
+           "ms_per_call": {k: [round(x, 2) for x in v[1:]] for k, v in call_ms.items()}}
 
     if rank != 0:
         if dist:

@@ -242,7 +242,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         // (Backprojection3D.cu:28-37)
         const ff dt2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
         const ff ds2 = ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb));
-        const ff lr2 = ff_div(D2, ff_sub(D2, ds2));
+        const ff den2 = ff_sub(D2, ds2);
+        const ff lr2 = ff_div_r(D2, den2, __fdividef(1.0f, den2.hi));
         const ff P2 = ff_mul(dt2, lr2);
         const float dect_s = ds2.hi, lr = lr2.hi, P = P2.hi;
         bool pin = P >= g.minp && P < g.maxp;
@@ -276,7 +277,9 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         bool zlimit = false;      // some z face limits a chord in this thread's range
         if (WMODE == W_CHORD) {
             const float dt = it + D * sb, ds = is - D * cb;
-            const float mt = ht * __frcp_rn(fabsf(dt)), ms = hs * __frcp_rn(fabsf(ds));
+            // approximate reciprocals (a few ulp): the chord factor needs ~1e-7, and the
+            // tie tests below have margins of 1e-5
+            const float mt = __fdividef(ht, fabsf(dt)), ms = __fdividef(hs, fabsf(ds));
             mts = fminf(mt, ms);
             qq = fmaf(dt, dt, ds * ds);
             zlimit = izmax * mts > hz;
@@ -289,7 +292,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
             bool tz1 = false, tz2 = false;
             float zc1 = 0.0f, zc2 = 0.0f;
             if (iz_vol * mts > 0.999f * hz) {
-                const float ztie = hz * __frcp_rn(mts);   // |iz| where the z faces tie with mts
+                const float ztie = __fdividef(hz, mts);   // |iz| where the z faces tie with mts
                 zc1 = (czf + ztie) * irz - 0.5f;
                 zc2 = (czf - ztie) * irz - 0.5f;
                 tz1 = fabsf(zc1 - rintf(zc1)) < 1e-3f;
@@ -320,7 +323,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         const float kc = 0.5f * (BP_ZC - 1);
         const float izc = fmaf(kc, rz, iz0);
         const float lc2 = fmaf(izc, izc, qq);
-        const float lc = sqrtf(lc2), ilc = 1.0f / lc;
+        const float ilc = rsqrtf(lc2), lc = lc2 * ilc;
         const float l1 = izc * rz * ilc, l2 = 0.5f * qq * rz * rz * ilc * ilc * ilc;
         const float hspan = kc * rz;
         const bool quad_ok = WMODE != W_CHORD ||

@@ -32,11 +32,17 @@ namespace ct {
 
 namespace {
 
+// Block 32 columns x 2 rows, 24 blocks (48 warps) per SM at 40 registers.
+// Measured at 512^3 / 360 views: 32 x 4 at 16 / 12 / 10 blocks per SM 47.6 (spills
+// at 32 registers) / 40.5 / 41.9 ms; 32 x 2 at 24 blocks 39.7 ms; 32 x 8 at 6
+// blocks 43.1 ms; the walk unrolled by 2 / 8 instead of 4: 41.7 / 41.5 ms.
 constexpr int FP_BX = 32;   // detector columns per block (one warp)
-constexpr int FP_BY = 4;    // detector rows per block
+#ifndef CT_FP_BY
+#define CT_FP_BY 2
+#endif
+constexpr int FP_BY = CT_FP_BY;   // detector rows per block
 #ifndef CT_FP_MINB
-#define CT_FP_MINB 12       // 48 warps per SM at 40 registers (measured at 512^3: 16 -> 47.6 ms with
-                            // spills at 32 registers, 12 -> 40.5 ms, 10 -> 41.9 ms)
+#define CT_FP_MINB 24
 #endif
 
 enum { COL_GRAZE = 1, COL_TPOS = 2, COL_TNEG = 4, COL_SPOS = 8, COL_SNEG = 16 };

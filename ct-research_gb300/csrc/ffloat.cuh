@@ -67,6 +67,15 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
     return ff_fast2sum(q1, __fdiv_rn(r.hi, b.hi));
 }
 
+// a / b from an approximate reciprocal r of b.hi (a few ulp): the remainder
+// a - q1 b is exact in float-float, so the first quotient's error is taken
+// back and the result is within ~2^-44 of a / b (relative)
+__device__ __forceinline__ ff ff_div_r(ff a, ff b, float r) {
+    const float q1 = __fmul_rn(a.hi, r);
+    const ff rem = ff_sub(a, ff_mul_f(b, q1));
+    return ff_fast2sum(q1, __fmul_rn(rem.hi, r));
+}
+
 // floor(a) for |a| < 2^31: floor of hi, one lower when hi is an integer and lo < 0
 __device__ __forceinline__ int ff_floor(ff a) {
     const float f = floorf(a.hi);
