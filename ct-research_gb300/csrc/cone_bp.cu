@@ -56,6 +56,10 @@ namespace {
 constexpr int BP_BX = 32;          // t per block
 constexpr int BP_BY = 4;           // s per block
 constexpr int BP_ZC = CT_BP_ZC;    // z per thread (register accumulators)
+static_assert(BP_ZC >= 1 && BP_ZC <= 64, "cone_bp: 1 to 64 z per thread");
+// bit k: z0 + k of the thread takes the view
+using zmask_t = std::conditional_t<(BP_ZC > 32), unsigned long long, unsigned>;
+constexpr zmask_t kZAll = BP_ZC >= 8 * (int)sizeof(zmask_t) ? ~zmask_t(0) : ((zmask_t(1) << BP_ZC) - 1);
 
 // Quads of nb views; R points at the first of them.
 __global__ void __launch_bounds__(256)
@@ -314,8 +318,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         if (WMODE == W_FDK_STICKY && kz < 0) r += (long long)kz * dqf;
         // z of this thread that take this view, as a bit mask over k
         const int klo = max(zlo - z0, 0), khi = min(((WMODE == W_FDK_STICKY) ? 0x7fff : zend) - z0, BP_ZC - 1);
-        const unsigned inmask = (klo > khi) ? 0u
-                                : ((khi >= 31 ? 0xffffffffu : ((2u << khi) - 1u)) & ~((1u << klo) - 1u));
+        const zmask_t inmask = (klo > khi) ? zmask_t(0)
+                               : ((khi >= BP_ZC - 1 ? kZAll : ((zmask_t(2) << khi) - 1)) & ~((zmask_t(1) << klo) - 1));
         // Fast path: every z of the thread takes the view, no z face limits the
         // chord, and the chord length |d| = sqrt(qq + iz^2) is the quadratic in k
         // about the thread's middle z (relative error below 1e-7, bounded by the
@@ -328,7 +332,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         const float hspan = kc * rz;
         const bool quad_ok = WMODE != W_CHORD ||
                              fabsf(izc) * hspan * hspan * hspan * ilc * ilc * ilc * ilc < 2e-7f;
-        const bool fast = inmask == 0xffffffffu && !zlimit && quad_ok &&
+        const bool fast = inmask == kZAll && !zlimit && quad_ok &&
                           !(WMODE == W_FDK_STICKY && kz < BP_ZC - 1);
         auto body = [&](auto fastpath) {
             constexpr bool FAST = decltype(fastpath)::value;
@@ -365,7 +369,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
                 if (FAST) {
                     acc[k] = fmaf(val, w, acc[k]);
                 } else {
-                    const bool in = (inmask >> k) & 1u;
+                    const bool in = (inmask >> k) & 1;
                     acc[k] = in ? fmaf(val, w, acc[k]) : acc[k];
                 }
             }
