@@ -157,10 +157,15 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
         const float sb = tr.x, cb = tr.y;
         const float P = fmaf(it, cb, is * sb);
         float Pd = P, u = 1.0f;
-        if (WMODE != BP2_FBPPAR) {
+        if (WMODE == BP2_FBPFAN) {
             const float S = fmaf(is, cb, -it * sb);
             u = (Rs - S) / Rs;
             Pd = P / u;
+        } else if (WMODE == BP2_BACKPROJ) {
+            // P / U = P Rs / (Rs - S): one division (the bin decision is re-taken in
+            // float-float near a boundary either way)
+            const float S = fmaf(is, cb, -it * sb);
+            Pd = __fdiv_rn(__fmul_rn(P, Rs), __fsub_rn(Rs, S));
         }
         float Plo = 0.0f;   // low part of Pd where it is recomputed in float-float
         const float qf = fabsf(Pd - g.p0) * ipint;
@@ -196,17 +201,22 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
             // edge lies ds_t = -ht ey / ex from the centre in s, and with the low s edge
             // dt_s = -hs ex / ey in t.  The reference's tests s in [0, s_high] and t in
             // [0, t_high] are decided on these small offsets, whose FP32 error is ~1e-7 of
-            // their size; within 1e-5 of a bound the FP64 construction decides.
-            const float ds_t = -ht * ey / ex;
+            // their size (approximate reciprocals, a few ulp); within 1e-5 of a bound the
+            // FP64 construction decides.
+            // (explicitly rounded products: no FMA contraction, so the single-slice and
+            // batched builds of this function give identical results)
+            const float iex = __fdividef(1.0f, ex);
+            const float ds_t = __fmul_rn(__fmul_rn(-ht, ey), iex);
             const float c1 = pcs + ds_t, c2 = hs - ds_t;           // s_at >= 0, s_at <= s_high
             bool tie = fabsf(c1) < 1e-5f * (pcs + fabsf(ds_t)) || fabsf(c2) < 1e-5f * (hs + fabsf(ds_t));
             bool none = false;
-            float a = (tlo - st) / ex;
+            float a = __fmul_rn(__fsub_rn(tlo, st), iex);
             if (!(c1 >= 0.0f && c2 >= 0.0f)) {
-                const float dt_s = -hs * ex / ey;
+                const float iey = __fdividef(1.0f, ey);
+                const float dt_s = __fmul_rn(__fmul_rn(-hs, ex), iey);
                 const float d1 = pct + dt_s, d2 = ht - dt_s;       // t_as >= 0, t_as <= t_high
                 tie = tie || fabsf(d1) < 1e-5f * (pct + fabsf(dt_s)) || fabsf(d2) < 1e-5f * (ht + fabsf(dt_s));
-                a = (slo - ss) / ey;
+                a = __fmul_rn(__fsub_rn(slo, ss), iey);
                 none = !(d1 >= 0.0f && d2 >= 0.0f);
             }
             if (tie) {
