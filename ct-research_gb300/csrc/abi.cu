@@ -910,6 +910,9 @@ bool host_pinned(const void *p) {
 // chunk overlaps the copy-out of the previous one, and the copy-in of a chunk
 // the backprojection of the previous one.
 constexpr int kDropinChunk = kFpViewChunk;
+// z slabs of the overlapped backprojection's last chunk, each copied out while
+// the next is summed (only the last slab's copy is left after the kernels)
+constexpr int kDropinSlabs = 4;
 
 // Reuse the cached cone plan when the geometry is unchanged.
 int cached_cone_plan(ct_cone_plan **out, int nt, int ns, int nz, const double *Size, const float *beta, int nb,
@@ -1022,9 +1025,13 @@ static int cone_bp_dropin(float *Display, const float *R, const float *xi, const
     const int bchunk = std::min(cone_bp_chunk_views(pl), kDropinChunk * 2);
     if (!fdk && nb > bchunk && np >= 2 && nx >= 2 && host_pinned(R) && host_pinned(Display)) {
         // pinned buffers: copy view chunks (the backprojector's own chunks) in,
-        // each backprojected (and added to the volume) while the next one arrives
+        // each backprojected (and added to the volume) while the next one arrives;
+        // the last chunk runs in z slabs, each copied out while the next is summed
         const int nchunks = (nb + bchunk - 1) / bchunk;
-        if ((s = dropin_streams(st, nchunks)) || (s = pl->quads.ensure(cone_quads_bytes(pl->g, bchunk)))) return s;
+        const int ztile = cone_bp_ztile(), ntiles = (nz + ztile - 1) / ztile;
+        const int nslab = std::min(kDropinSlabs, ntiles);
+        if ((s = dropin_streams(st, nchunks + nslab)) || (s = pl->quads.ensure(cone_quads_bytes(pl->g, bchunk))))
+            return s;
         const size_t per_view = (size_t)np * nx;
         for (int c = 0; c < nchunks; ++c) {
             const int v0 = c * bchunk, n = std::min(bchunk, nb - v0);
@@ -1035,14 +1042,28 @@ static int cone_bp_dropin(float *Display, const float *R, const float *xi, const
         }
         for (int c = 0; c < nchunks; ++c) {
             const int v0 = c * bchunk, n = std::min(bchunk, nb - v0);
+            const bool last = c == nchunks - 1;
             CT_CUDA(cudaStreamWaitEvent(st.cs, st.ev[c], 0), "event wait");
-            if ((s = cone_pack_quads(pl->g, st.proj.as<float>(), pl->quads.as<float4>(), v0, n, st.cs)) ||
-                (s = cone_bp_launch(pl->g, pl->quads.as<float4>(), v0, n, c == 0 ? nullptr : st.vol.as<float>(),
-                                    st.vol.as<float>(), 0, nullptr, 0.f, 0.f, 0.f, 0.f, false, st.cs)))
-                return s;
+            if ((s = cone_pack_quads(pl->g, st.proj.as<float>(), pl->quads.as<float4>(), v0, n, st.cs))) return s;
+            for (int k = 0; k < (last ? nslab : 1); ++k) {
+                const int t0 = last ? k * ntiles / nslab : 0, t1 = last ? (k + 1) * ntiles / nslab : ntiles;
+                if ((s = cone_bp_launch(pl->g, pl->quads.as<float4>(), v0, n, c == 0 ? nullptr : st.vol.as<float>(),
+                                        st.vol.as<float>(), 0, nullptr, 0.f, 0.f, 0.f, 0.f, false, st.cs, t0,
+                                        t1 - t0)))
+                    return s;
+                if (last) {
+                    // slices [t0, t1) * ztile are final: copy them out behind the next slab
+                    const size_t slice = (size_t)nt * ns, za = (size_t)t0 * ztile,
+                                 zb = std::min<size_t>(nz, (size_t)t1 * ztile);
+                    CT_CUDA(cudaEventRecord(st.ev[nchunks + k], st.cs), "event");
+                    CT_CUDA(cudaStreamWaitEvent(st.xs, st.ev[nchunks + k], 0), "event wait");
+                    CT_CUDA(cudaMemcpyAsync(Display + za * slice, st.vol.as<float>() + za * slice,
+                                            (zb - za) * slice * sizeof(float), cudaMemcpyDeviceToHost, st.xs),
+                            "D2H volume");
+                }
+            }
         }
-        CT_CUDA(cudaMemcpyAsync(Display, st.vol.ptr, nv * sizeof(float), cudaMemcpyDeviceToHost, st.cs),
-                "D2H volume");
+        CT_CUDA(cudaStreamSynchronize(st.xs), "sync");
         CT_CUDA(cudaStreamSynchronize(st.cs), "sync");
         return CT_OK;
     }

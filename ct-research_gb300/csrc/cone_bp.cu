@@ -199,7 +199,7 @@ __device__ __noinline__ int chord_end_z(const ConeGeom &g, int ti, int si, doubl
 template <int WMODE, bool UPDATE>
 __global__ void __launch_bounds__(BP_BX * BP_BY, WMODE == W_CHORD ? CT_BP_MINB : CT_BP_MINB_FDK)
 cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, const float *prev, float *out,
-               const float *__restrict__ colsum, float eps, float lambda, float lo, float hi) {
+               const float *__restrict__ colsum, float eps, float lambda, float lo, float hi, int zt0) {
     // the row table (x - q(xi[x]), q(xi[x+1]) - x) of ConeGeom::xtab
     extern __shared__ float2 xtab[];
     const int tid = threadIdx.x + BP_BX * threadIdx.y;
@@ -208,7 +208,7 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
 
     const int ti = blockIdx.x * BP_BX + threadIdx.x;
     const int si = blockIdx.y * BP_BY + threadIdx.y;
-    const int z0 = blockIdx.z * BP_ZC;
+    const int z0 = (zt0 + (int)blockIdx.z) * BP_ZC;
     if (ti >= g.nt || si >= g.ns) return;
 
     // voxel-centre coordinates relative to the rotation centre, exact to ~2^-48
@@ -405,17 +405,23 @@ int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, int v0, int nv
     return CT_OK;
 }
 
+int cone_bp_ztile() { return BP_ZC; }
+
 // weighting: 0 chord, 1 FDK (off-detector adds 0), 2 FDK sticky
 int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const float *prev, float *out, int weighting,
-                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st) {
+                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st,
+                   int zt0, int nzt) {
     CT_REQUIRE(g.np >= 2 && g.nx >= 2, "cone_bp: detector needs at least 2x2 samples");
     CT_REQUIRE(v0 >= 0 && nv > 0 && v0 + nv <= g.nb, "cone_bp: view range out of bounds");
+    const int ntiles = (g.nz + BP_ZC - 1) / BP_ZC;
+    if (nzt <= 0) nzt = ntiles - zt0;
+    CT_REQUIRE(zt0 >= 0 && nzt > 0 && zt0 + nzt <= ntiles, "cone_bp: z tile range out of bounds");
     dim3 block(BP_BX, BP_BY);
-    dim3 grid((g.nt + BP_BX - 1) / BP_BX, (g.ns + BP_BY - 1) / BP_BY, (g.nz + BP_ZC - 1) / BP_ZC);
+    dim3 grid((g.nt + BP_BX - 1) / BP_BX, (g.ns + BP_BY - 1) / BP_BY, nzt);
     const size_t smem = sizeof(float2) * (size_t)g.nx;
     CT_REQUIRE(smem <= 48 * 1024, "cone_bp: at most 6144 detector rows");
 #define CT_BP_CASE(W, U)                                                                     \
-    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, v0, nv, prev, out, colsum, eps, lambda, lo, hi)
+    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, v0, nv, prev, out, colsum, eps, lambda, lo, hi, zt0)
     if (update) {
         if (weighting == W_CHORD) CT_BP_CASE(W_CHORD, true);
         else if (weighting == W_FDK_ZERO) CT_BP_CASE(W_FDK_ZERO, true);

@@ -108,8 +108,11 @@ int fan_fixup_launch(const FanGeom &g, const float *img, void *out, bool out_dou
 // clamp(vol + lambda * sum / (colsum + eps), lo, hi).
 size_t cone_quads_bytes(const ConeGeom &g, int nviews);
 int cone_pack_quads(const ConeGeom &g, const float *R, float4 *Q, int v0, int nv, cudaStream_t st);
+// zt0, nzt: a range of z tiles of cone_bp_ztile() slices (nzt = 0: from zt0 to the top).
 int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const float *prev, float *out, int weighting,
-                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st);
+                   const float *colsum, float eps, float lambda, float lo, float hi, bool update, cudaStream_t st,
+                   int zt0 = 0, int nzt = 0);
+int cone_bp_ztile();
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st);
 int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);

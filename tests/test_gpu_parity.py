@@ -322,13 +322,15 @@ def test_bp_view_chunks_match_one_pass(oracle, torch_cuda):
 def test_dropin_pinned_overlap_matches_pageable(torch_cuda):
     """Pinned host buffers take the overlapped drop-in path (view chunks copied
     out while the next chunk is projected, copied in while the previous one is
-    backprojected).  The forward projection is the same arithmetic per ray, so
-    bit-identical to the pageable path; the backprojection adds chunk sums in
-    float, so it differs from one pass only by rounding."""
+    backprojected; the last chunk runs in z slabs, each copied out while the
+    next is summed: 80 slices make three slabs).  The forward projection is the
+    same arithmetic per ray, so bit-identical to the pageable path; the
+    backprojection adds chunk sums in float, so it differs from one pass only
+    by rounding."""
     import ctypes as C
     from ctgb import _lib
     torch = torch_cuda
-    geom, vol = _random_cone(17, shape=(24, 28, 32), nb=200, np_=40, nx=24)
+    geom, vol = _random_cone(17, shape=(80, 28, 32), nb=200, np_=40, nx=24)
     lib = _lib.lib()
     res = np.array([geom.size[0] / geom.nt, geom.size[1] / geom.ns, geom.size[2] / geom.nz])
     size = np.array(geom.size, dtype=np.float64)
