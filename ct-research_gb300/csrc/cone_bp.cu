@@ -219,6 +219,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
     const ff ipint2 = ff_from(1.0 / (double)g.pint);
     const ff xq2 = ff_from((double)g.xsgn / (double)g.xint);   // row quotient per mm of xi
     const ff p02 = {g.p0, 0.0f}, x02 = {g.x0, 0.0f};
+    // the view-independent factors of the row quotient: (iz lr - xi0) xq = lr (iz xq) - xi0 xq
+    const ff rzxq2 = ff_mul(rz2, xq2), iz0xq2 = ff_mul(iz02, xq2), x0xq2 = ff_mul(x02, xq2);
 
     const float rz = (float)g.res[2];
     const float it = it2.hi, is = is2.hi;
@@ -273,8 +275,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         // row quotient q(z) = |xi(z) - xi[0]| / XigamaInt, affine in z, as 64-bit
         // fixed point (32 fraction bits): floor and weights follow the
         // reference's FP64 values except within ~1e-8 of a row boundary
-        const long long dqf = ff_fixed32(ff_mul(ff_mul(rz2, lr2), xq2));
-        long long r = ff_fixed32(ff_mul(ff_sub(ff_mul(iz02, lr2), x02), xq2));
+        const long long dqf = ff_fixed32(ff_mul(rzxq2, lr2));
+        long long r = ff_fixed32(ff_sub(ff_mul(iz0xq2, lr2), x0xq2));
 
         float wv = 1.0f, mts = 0.0f, qq = 0.0f;
         int zend = zhi;           // last z that receives this view's value
@@ -330,8 +332,13 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
         const float ilc = rsqrtf(lc2), lc = lc2 * ilc;
         const float l1 = izc * rz * ilc, l2 = 0.5f * qq * rz * rz * ilc * ilc * ilc;
         const float hspan = kc * rz;
+        // more than 32 z: a cubic term, whose error (fourth order) is below
+        // h^4 / (2 |d|^4)
+        const float l3 = (BP_ZC > 32) ? -0.5f * qq * izc * rz * rz * rz * ilc * ilc * ilc * ilc * ilc : 0.0f;
+        const float hl = hspan * ilc;
         const bool quad_ok = WMODE != W_CHORD ||
-                             fabsf(izc) * hspan * hspan * hspan * ilc * ilc * ilc * ilc < 2e-7f;
+                             ((BP_ZC > 32) ? 0.5f * hl * hl * hl * hl < 2e-7f
+                                           : fabsf(izc) * hspan * hspan * hspan * ilc * ilc * ilc * ilc < 2e-7f);
         const bool fast = inmask == kZAll && !zlimit && quad_ok &&
                           !(WMODE == W_FDK_STICKY && kz < BP_ZC - 1);
         auto body = [&](auto fastpath) {
@@ -357,7 +364,8 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
                     // min(1, hz / (|iz| mts)) is 1 where no z face limits the chord
                     if (FAST) {
                         const float dk = (float)k - kc;
-                        w = fmaf(dk, fmaf(dk, l2, l1), lc);
+                        if constexpr (BP_ZC > 32) w = fmaf(dk, fmaf(dk, fmaf(dk, l3, l2), l1), lc);
+                        else w = fmaf(dk, fmaf(dk, l2, l1), lc);
                     } else {
                         const float iz = fmaf((float)k, rz, iz0);
                         const float d2 = fmaf(iz, iz, qq);
