@@ -162,10 +162,11 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
             u = (Rs - S) / Rs;
             Pd = P / u;
         } else if (WMODE == BP2_BACKPROJ) {
-            // P / U = P Rs / (Rs - S): one division (the bin decision is re-taken in
-            // float-float near a boundary either way)
+            // P / U = P Rs / (Rs - S), approximate division (2 ulp): with the products'
+            // rounding Pd is within ~4 ulp, inside the margin below, and the bin
+            // decision is re-taken in float-float near a boundary either way
             const float S = fmaf(is, cb, -it * sb);
-            Pd = __fdiv_rn(__fmul_rn(P, Rs), __fsub_rn(Rs, S));
+            Pd = __fdividef(__fmul_rn(P, Rs), __fsub_rn(Rs, S));
         }
         float Plo = 0.0f;   // low part of Pd where it is recomputed in float-float
         const float qf = fabsf(Pd - g.p0) * ipint;
