@@ -1223,6 +1223,7 @@ static int batch_layout(ct_fan_batch *b) {
     for (size_t k = 0; k < b->plans.size(); ++k) {
         BatchSlice &s = b->h[k];
         s.g = b->plans[k]->g;
+        fan_geom_derive(s.g);
         s.img_off = io;
         s.sino_off = so;
         s.ray_blk0 = (int)fb;

@@ -57,8 +57,10 @@ fan_bp_kernel(const FanGeom g, const float *__restrict__ R, float *__restrict__ 
 }  // namespace
 
 // mode 0: forward projection (float); 1: residual (float); 3: forward projection into double
-int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
+int fan_fp_launch(const FanGeom &g0, const float *img, void *out, const float *b, const float *rowsum,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {
+    FanGeom g = g0;
+    fan_geom_derive(g);
     const long long nray = (long long)g.nb * g.np;
     const unsigned blocks = (unsigned)((nray + F2_BLOCK - 1) / F2_BLOCK);
     CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");

@@ -53,7 +53,8 @@ __device__ __forceinline__ bool fan_ray_setup(const FanGeom &g, long long r, Ray
     }
     src[2] = 0.5;
     d[2] = 0.0;
-    return siddon_setup(src, d, n, res, w);
+    const double ires[3] = {g.ires[0], g.ires[1], 1.0}, ext[3] = {g.ext[0], g.ext[1], 1.0};
+    return siddon_setup(src, d, n, res, ires, ext, w);
 }
 
 // Line integral of ray r = view * np + bin; sets `grazing` for rays the FP64

@@ -19,7 +19,18 @@ struct FanGeom {
     float pint, bint, minp, maxp, p0, psgn;
     int parallel;            // 1: parallel-beam geometry
     double smax;             // parallel: max |t| (ProjectionParallel_2D.cu:25)
+    // derived on the host before each launch of the forward walk (fan_geom_derive):
+    // 1 / res and n * res per axis, so the per-ray set-up divides nothing
+    double ires[2], ext[2];
 };
+
+inline void fan_geom_derive(FanGeom &g) {
+    const int n[2] = {g.nt, g.ns};
+    for (int a = 0; a < 2; ++a) {
+        g.ires[a] = 1.0 / g.res[a];
+        g.ext[a] = n[a] * g.res[a];
+    }
+}
 
 // Detector-row filter job (filter.cu).
 struct RowFilter {

@@ -27,15 +27,18 @@ struct RayWalk {
 };
 
 // FP64 slab test against the box [0, n*res] and walk set-up for the line
-// src + alpha * d.  Returns false for lines that miss the box.
+// src + alpha * d.  Returns false for lines that miss the box.  ires = 1 / res
+// and ext = n * res per axis, as the host computes them (IEEE double, the same
+// values a device division would give).
 __device__ __forceinline__ bool siddon_setup(const double src[3], const double d[3], const int n[3],
-                                             const double res[3], RayWalk &w) {
+                                             const double res[3], const double ires[3], const double ext[3],
+                                             RayWalk &w) {
     double inv[3];
     double a_in = -1.0e300, a_out = 1.0e300;
     int ax_in = -1, ax_out = -1;   // axes whose faces the line enters and leaves through
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double hi = n[a] * res[a];
+        const double hi = ext[a];
         if (d[a] != 0.0) {
             inv[a] = drcp(d[a]);
             const double t0 = (0.0 - src[a]) * inv[a];
@@ -55,7 +58,7 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
     bool grazing = false;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double ir = 1.0 / res[a];
+        const double ir = ires[a];
         const double gin = (src[a] + a_in * d[a]) * ir;
         const double gout = (src[a] + a_out * d[a]) * ir;
         // nearly parallel to the planes of this axis and within reach of one:

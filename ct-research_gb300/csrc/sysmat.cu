@@ -110,8 +110,10 @@ int cone_sysmat_launch(const ConeGeom &g, int v0, int nv, long long *row_ptr, in
     return cone_sysmat_ref_launch(g, r0, row_ptr, col, val, fill, gl, st);
 }
 
-int fan_sysmat_launch(const FanGeom &g, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
+int fan_sysmat_launch(const FanGeom &g0, long long *row_ptr, int *col, float *val, bool fill, const GrazeList &gl,
                       cudaStream_t st) {
+    FanGeom g = g0;
+    fan_geom_derive(g);
     CT_CUDA(cudaMemsetAsync(gl.count, 0, sizeof(*gl.count), st), "graze list reset");
     const long long rays = (long long)g.nb * g.np;
     const unsigned blocks = (unsigned)((rays + 127) / 128);
