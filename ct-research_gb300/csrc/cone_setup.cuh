@@ -1,6 +1,9 @@
-// cone_setup.cuh -- Siddon walk set-up of one cone-beam ray, shared by the
-// forward projector (cone_fp.cu) and the system-matrix export (sysmat.cu) so
-// that both walk exactly the same segments.
+// cone_setup.cuh -- Siddon walk set-up of one cone-beam ray on its own, for
+// the system-matrix export (sysmat.cu) and the segment count (cone_fp.cu).
+// The forward projector takes the in-plane part of the same set-up from a
+// per-column table (cone_fp.cu); both follow the same face and voxel rules,
+// so their segments differ at most by float rounding of the crossing
+// parameters (A x matches the projection to ~1e-7).
 #pragma once
 #include "kernels.cuh"
 #include "siddon.cuh"

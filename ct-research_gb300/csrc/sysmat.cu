@@ -3,8 +3,8 @@
 // The reference builds its system matrices on the CPU in MATLAB
 // (GenSysMatFan.m, GenSysMatParal.m, GenSysMatCircular3D.m: a Siddon walk per
 // ray, sparse(L, J, W)), and SIRT.m iterates with them (SIRT.m:79).  Here the
-// rows come from the GPU tracer itself: each ray is walked with the set-up
-// and the walk of the forward projector (cone_setup.cuh, fan2d_dev.cuh,
+// rows come from the GPU tracer itself: each ray is walked with the forward
+// projectors' face and voxel rules and walk (cone_setup.cuh, fan2d_dev.cuh,
 // siddon.cuh), so A x equals the projector's output to float rounding, and
 // rays that graze a grid plane are walked by the FP64 reference walk as the
 // projector does (ref_walk.cu).  Rows are rays in sinogram order, columns
