@@ -19,9 +19,11 @@
 // smoothing window runs over each finished filtered row.
 //
 // One block per row; the row, its mixed copy and the taps live in shared
-// memory.  Partial sums run in FP32 and are flushed into a double every 128
-// taps; each chunk result is added into the float output as the reference's
-// `dev_Rcov[...] += PInt * Rcovsum` does.
+// memory.  A thread computes FJ consecutive outputs: the taps they need at
+// one input sample are consecutive, so one tap load per sample slides a
+// register window.  Partial sums are exact float pairs flushed into a double
+// every 256 taps; each chunk result is added into the float output as the
+// reference's `dev_Rcov[...] += PInt * Rcovsum` does.
 #include "kernels.cuh"
 
 namespace ct {
@@ -30,6 +32,12 @@ namespace ct {
 namespace {
 
 constexpr int FT = 256;
+// measured at 256^3 FDK (360 x 384 rows of 512): 2 / 4 / 8 outputs per thread
+// 10.47 / 8.90 / 9.00 ms; one output per thread (two tap loads per product) 11.75 ms
+#ifndef CT_FILTER_FJ
+#define CT_FILTER_FJ 4
+#endif
+constexpr int FJ = CT_FILTER_FJ;   // consecutive outputs per thread
 
 __global__ void __launch_bounds__(FT)
 row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restrict__ out) {
@@ -47,7 +55,7 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
         raw[q] = pw ? __fmul_rn(in[q], pw[q]) : in[q];
         o[q] = 0.0f;
     }
-    for (int q = threadIdx.x; q < 2 * np - 1; q += blockDim.x) G[q] = f.G[q];
+    for (int q = threadIdx.x; q < 2 * np - 1 + FJ; q += blockDim.x) G[q] = q < 2 * np - 1 ? f.G[q] : 0.0f;
     __syncthreads();
 
     const int gtime = (np + f.limit - 1) / f.limit;
@@ -85,29 +93,50 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
                 mix[q] = v;
             }
             __syncthreads();
-            for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+            for (int pb = p0 + FJ * threadIdx.x; pb < p1; pb += FJ * blockDim.x) {
                 // The reference rounds each float*float product to float and sums
                 // in double (FDK.cu:41-45).  Here: the same rounded products,
-                // summed as an unevaluated pair (s + c) with the TwoSum error-free
-                // transformation (Knuth), flushed into a double every 256 taps.
-                double dacc = 0.0;
-                const float *gp = G + (np - 1) + p;
+                // summed per output as an unevaluated pair (s + c) with the TwoSum
+                // error-free transformation (Knuth), flushed into a double every
+                // 256 taps.  Output pb + j takes tap G[(np - 1) + pb + j - q] at
+                // sample q: the window w[j] of the FJ outputs moves by one tap per
+                // sample (G carries FJ zeros past its end for the window's start).
+                double dacc[FJ];
+#pragma unroll
+                for (int j = 0; j < FJ; ++j) dacc[j] = 0.0;
+                const float *gp = G + (np - 1) + pb;
                 // chunks of 256 taps keep the double flush out of the inner loop
                 for (int q0 = g0; q0 < g1; q0 += 256) {
                     const int q1 = min(q0 + 256, g1);
-                    float sh = 0.0f, sl = 0.0f;
+                    float sh[FJ], sl[FJ], w[FJ];
+#pragma unroll
+                    for (int j = 0; j < FJ; ++j) {
+                        sh[j] = 0.0f;
+                        sl[j] = 0.0f;
+                        w[j] = gp[j + 1 - q0];   // the window of sample q0 - 1
+                    }
 #pragma unroll 4
                     for (int q = q0; q < q1; ++q) {
-                        const float prod = __fmul_rn(mix[q], gp[-q]);
-                        const float t = __fadd_rn(sh, prod);
-                        const float bp = __fsub_rn(t, sh);
-                        const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(prod, bp));
-                        sh = t;
-                        sl = __fadd_rn(sl, err);
+#pragma unroll
+                        for (int j = FJ - 1; j > 0; --j) w[j] = w[j - 1];
+                        w[0] = gp[-q];
+                        const float m = mix[q];
+#pragma unroll
+                        for (int j = 0; j < FJ; ++j) {
+                            const float prod = __fmul_rn(m, w[j]);
+                            const float t = __fadd_rn(sh[j], prod);
+                            const float bp = __fsub_rn(t, sh[j]);
+                            const float err = __fadd_rn(__fsub_rn(sh[j], __fsub_rn(t, bp)), __fsub_rn(prod, bp));
+                            sh[j] = t;
+                            sl[j] = __fadd_rn(sl[j], err);
+                        }
                     }
-                    dacc += (double)sh + (double)sl;
+#pragma unroll
+                    for (int j = 0; j < FJ; ++j) dacc[j] += (double)sh[j] + (double)sl[j];
                 }
-                o[p] = (float)((double)o[p] + (double)f.pint * dacc);
+#pragma unroll
+                for (int j = 0; j < FJ; ++j)
+                    if (pb + j < p1) o[pb + j] = (float)((double)o[pb + j] + (double)f.pint * dacc[j]);
             }
             __syncthreads();
         }
@@ -133,13 +162,14 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
 
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st) {
     CT_REQUIRE(f.np >= 2, "row filter: at least 2 detector samples");
-    const size_t smem = sizeof(float) * (size_t)(4 * f.np - 1);
+    const size_t smem = sizeof(float) * (size_t)(4 * f.np - 1 + FJ);
     CT_REQUIRE(smem <= 200 * 1024, "row filter: detector row too long for shared memory");
     if (smem > 48 * 1024)
         CT_CUDA(cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                 "row_filter smem attribute");
-    // launch order: one thread per output of a P-tile, so no thread idles at the tile barriers
-    const int block = (f.launch_order && f.w) ? std::min(FT, std::max(32, (f.tile + 31) / 32 * 32)) : FT;
+    // FJ outputs per thread over a P-tile (launch order) or the row, so no thread idles
+    const int span = (f.launch_order && f.w) ? f.tile : f.np;
+    const int block = std::min(FT, std::max(32, ((span + FJ - 1) / FJ + 31) / 32 * 32));
     row_filter_kernel<<<f.nrow, block, smem, st>>>(f, R, out);
     CT_LAUNCH_CHECK("row_filter_kernel");
     return CT_OK;
