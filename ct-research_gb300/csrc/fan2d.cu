@@ -75,8 +75,10 @@ int fan_fp_launch(const FanGeom &g0, const float *img, void *out, const float *b
 }
 
 // wmode: 0 BackprojectionFan2D weight, 1 FBPfan, 2 FBPpara
-int fan_bp_launch(const FanGeom &g, const float *R, float *img, int wmode, const float *colsum, float eps,
+int fan_bp_launch(const FanGeom &g0, const float *R, float *img, int wmode, const float *colsum, float eps,
                   float lambda, float lo, float hi, bool update, cudaStream_t st) {
+    FanGeom g = g0;
+    fan_geom_derive(g);
     CT_REQUIRE(g.np >= 2, "fan_bp: at least 2 detector bins");
     const unsigned blocks = (unsigned)((g.nt * g.ns + F2_BLOCK - 1) / F2_BLOCK);
 #define CT_F2_CASE(W, U) fan_bp_kernel<W, U><<<blocks, F2_BLOCK, 0, st>>>(g, R, img, colsum, eps, lambda, lo, hi)

@@ -113,14 +113,17 @@ __device__ __forceinline__ bool ff_lt(ff a, float b) { return a.hi < b || (a.hi 
 
 // The reference's detector coordinate P / U of pixel (ti, si) in one view in
 // float-float (ffloat.cuh), for the pixel-views where the FP32 value lies near
-// a decision boundary.  One division, by a reciprocal and a float-float
-// correction.
+// a decision boundary.  The pixel centre (ti + 1/2) res - size / 2 comes from
+// the geometry's float-float constants (fan_geom_derive), so this runs no
+// FP64.  One division, by a reciprocal and a float-float correction.
 static __device__ __noinline__ ff fan_pd_ff(const FanGeom &g, int ti, int si, float sb, float cb, int wmode) {
-    const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
-    const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
+    const ff it2 = ff_sub(ff_mul_f(ff{g.res_ff[0].x, g.res_ff[0].y}, (float)ti + 0.5f),
+                          ff{g.hsize_ff[0].x, g.hsize_ff[0].y});
+    const ff is2 = ff_sub(ff_mul_f(ff{g.res_ff[1].x, g.res_ff[1].y}, (float)si + 0.5f),
+                          ff{g.hsize_ff[1].x, g.hsize_ff[1].y});
     const ff P2 = ff_add(ff_mul_f(it2, cb), ff_mul_f(is2, sb));
     if (wmode == BP2_FBPPAR) return P2;
-    const ff R2 = ff_from(g.D);
+    const ff R2 = {g.D_ff.x, g.D_ff.y};
     const ff den = ff_sub(R2, ff_sub(ff_mul_f(is2, cb), ff_mul_f(it2, sb)));   // Rscan - S
     const ff num = ff_mul(P2, R2);                                             // P / ((Rscan - S) / Rscan)
     const float r = __frcp_rn(den.hi);
@@ -182,7 +185,7 @@ __device__ __forceinline__ float fan_pixel_sum(const FanGeom &g, const float *__
         float val = 0.0f;
         if (ff_ge(Pd2, g.minp) && ff_lt(Pd2, g.maxp)) {
             // far from a bin boundary the FP32 quotient has the reference's floor
-            int p1 = near ? ff_floor(ff_mul(ff_abs(ff_sub(Pd2, ff{g.p0, 0.0f})), ff_from(1.0 / (double)g.pint)))
+            int p1 = near ? ff_floor(ff_mul(ff_abs(ff_sub(Pd2, ff{g.p0, 0.0f})), ff{g.ipint_ff.x, g.ipint_ff.y}))
                           : (int)qf;
             p1 = min(max(p1, 0), g.np - 2);
             const float pa = __ldg(g.Pf + p1), pb = __ldg(g.Pf + p1 + 1);

@@ -19,17 +19,29 @@ struct FanGeom {
     float pint, bint, minp, maxp, p0, psgn;
     int parallel;            // 1: parallel-beam geometry
     double smax;             // parallel: max |t| (ProjectionParallel_2D.cu:25)
-    // derived on the host before each launch of the forward walk (fan_geom_derive):
-    // 1 / res and n * res per axis, so the per-ray set-up divides nothing
+    // derived on the host before each launch (fan_geom_derive): 1 / res and n * res
+    // per axis, so the per-ray set-up divides nothing; and float-float (hi, lo)
+    // copies of res, size / 2, D and 1 / pint for the backprojector's
+    // near-boundary recompute, so that it runs no FP64
     double ires[2], ext[2];
+    float2 res_ff[2], hsize_ff[2], D_ff, ipint_ff;
 };
+
+inline float2 ff_split_host(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
 
 inline void fan_geom_derive(FanGeom &g) {
     const int n[2] = {g.nt, g.ns};
     for (int a = 0; a < 2; ++a) {
         g.ires[a] = 1.0 / g.res[a];
         g.ext[a] = n[a] * g.res[a];
+        g.res_ff[a] = ff_split_host(g.res[a]);
+        g.hsize_ff[a] = ff_split_host(0.5 * g.size[a]);
     }
+    g.D_ff = ff_split_host(g.D);
+    g.ipint_ff = ff_split_host(1.0 / (double)g.pint);
 }
 
 // Detector-row filter job (filter.cu).
