@@ -53,6 +53,11 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
     }
     if (!(a_out > a_in)) return false;
 
+    // FP32 copies of d (for |d| in FP32)
+    const float L = (float)(a_out - a_in);
+    float df[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) df[a] = (float)d[a];
     int vs[3], cnt[3], sg[3];
     float a0[3], da[3];
     bool grazing = false;
@@ -61,13 +66,15 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
         const double ir = ires[a];
         const double gin = (src[a] + a_in * d[a]) * ir;
         const double gout = (src[a] + a_out * d[a]) * ir;
+        // signs from the bits (no FP64 compare)
+        const long long db = __double_as_longlong(d[a]);
+        sg[a] = (db << 1) == 0 ? 0 : (db < 0 ? -1 : 1);
         // nearly parallel to the planes of this axis and within reach of one:
         // the reference's charge then depends on FP64 rounding of a clamped slope
-        if (d[a] != 0.0) {
+        if (sg[a] != 0 && fabs(gout - gin) < 1e-3) {
             const double glo = fmin(gin, gout), ghi = fmax(gin, gout);
-            if (ghi - glo < 1e-3 && floor(ghi + 1e-9) != floor(glo - 1e-9)) grazing = true;
+            if (floor(ghi + 1e-9) != floor(glo - 1e-9)) grazing = true;
         }
-        sg[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
         // On the entry / exit face the voxel is known exactly; on the other axes
         // the voxel is the floor of the coordinate, as the reference's
         // midpoint-floor rule gives for lines along a grid plane.
@@ -97,8 +104,8 @@ __device__ __forceinline__ bool siddon_setup(const double src[3], const double d
     w.idx = (vs[2] * n[1] + vs[1]) * n[0] + vs[0];
     w.nseg = 1 + cnt[0] + cnt[1] + cnt[2];
     w.grazing = grazing;
-    w.L = (float)(a_out - a_in);
-    w.scale = (float)sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    w.L = L;
+    w.scale = sqrtf(fmaf(df[0], df[0], fmaf(df[1], df[1], df[2] * df[2])));
     return true;
 }
 
