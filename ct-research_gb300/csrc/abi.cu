@@ -650,12 +650,13 @@ int ct_cone_count_segments(ct_cone_plan *plan, long long *segments, void *stream
 // ---------------------------------------------------------------------------
 struct ct_fan_plan {
     FanGeom g{};
-    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, pwt, win, scan;
+    DevBuf trig_d, Pd, trig_f, Pf, G, wtab, rcov, pwt, win, scan, rays;
     GrazeBuf graze;
     std::vector<float> hPf, hbf;
     FilterOpts filt;
     double wsum = 0.0;
     ~ct_fan_plan() {
+        rays.release();
         trig_d.release(); Pd.release(); trig_f.release(); Pf.release();
         G.release(); wtab.release(); rcov.release(); graze.release(); pwt.release(); win.release(); scan.release();
     }
@@ -717,12 +718,29 @@ static int fan_plan_make(ct_fan_plan **out, int nt, int ns, const double size2[2
     return CT_OK;
 }
 
+// The forward walk's set-up table of a plan (48 bytes per ray), built once the
+// geometry is final, synchronously (no later launch or graph capture can
+// precede it).  The one-call drop-ins skip it and set rays up per call.
+static int fan_ray_table(ct_fan_plan *pl) {
+    const FanGeom &g = pl->g;
+    int s = pl->rays.ensure(sizeof(FanRay) * (size_t)g.nb * g.np);
+    if (s || (s = fan_ray_table_launch(g, pl->rays.as<FanRay>(), nullptr))) return s;
+    CT_CUDA(cudaStreamSynchronize(nullptr), "ray set-up table");
+    pl->g.ray_tab = pl->rays.as<FanRay>();
+    return CT_OK;
+}
+
 extern "C" {
 
 int ct_fan_plan_create(ct_fan_plan **plan, int nt, int ns, const double *Size, const double *beta, int nb,
                        const double *P, int np, double D) {
     CT_REQUIRE(Size, "Size is null");
-    return fan_plan_make(plan, nt, ns, Size, beta, nb, P, np, D, 0);
+    int s = fan_plan_make(plan, nt, ns, Size, beta, nb, P, np, D, 0);
+    if (!s && (s = fan_ray_table(*plan))) {
+        delete *plan;
+        *plan = nullptr;
+    }
+    return s;
 }
 
 int ct_fan_plan_destroy(ct_fan_plan *plan) {
@@ -740,7 +758,11 @@ int ct_par_plan_create(ct_fan_plan **plan, int height, int width, const double *
     if (s) return s;
     (*plan)->g.res[0] = resolution[1];
     (*plan)->g.res[1] = resolution[0];
-    return CT_OK;
+    if ((s = fan_ray_table(*plan))) {
+        delete *plan;
+        *plan = nullptr;
+    }
+    return s;
 }
 
 int ct_fan_sysmat(ct_fan_plan *plan, long long *d_row_ptr, int *d_col, float *d_val, long long cap, long long *nnz,

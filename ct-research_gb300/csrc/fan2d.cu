@@ -56,6 +56,33 @@ fan_bp_kernel(const FanGeom g, const float *__restrict__ R, float *__restrict__ 
 
 }  // namespace
 
+// The set-up table: ray r's walk set-up as fan_ray_setup_compute makes it.
+__global__ void __launch_bounds__(256)
+fan_ray_table_kernel(const FanGeom g, FanRay *__restrict__ tab) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= (long long)g.nb * g.np) return;
+    RayWalk w;
+    const bool hit = fan_ray_setup_compute(g, r, w);
+    FanRay t;
+    t.a0t = w.a0; t.a0s = w.a1; t.dat = w.d0; t.das = w.d1;
+    t.L = w.L; t.scale = w.scale;
+    t.idx = w.idx; t.nseg = w.nseg;
+    t.st = w.s0; t.ss = w.s1;
+    t.flags = (hit ? 1 : 0) | (w.grazing ? 2 : 0);
+    t.pad_ = 0;
+    tab[r] = t;
+}
+
+int fan_ray_table_launch(const FanGeom &g0, FanRay *tab, cudaStream_t st) {
+    FanGeom g = g0;
+    fan_geom_derive(g);
+    g.ray_tab = nullptr;
+    const long long n = (long long)g.nb * g.np;
+    fan_ray_table_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, tab);
+    CT_LAUNCH_CHECK("fan_ray_table_kernel");
+    return CT_OK;
+}
+
 // mode 0: forward projection (float); 1: residual (float); 3: forward projection into double
 int fan_fp_launch(const FanGeom &g0, const float *img, void *out, const float *b, const float *rowsum,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st) {

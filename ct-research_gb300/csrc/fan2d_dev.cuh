@@ -30,8 +30,8 @@ namespace ct {
 
 enum { BP2_BACKPROJ = 0, BP2_FBPFAN = 1, BP2_FBPPAR = 2 };
 
-// Walk set-up of ray r = view * np + bin; false for rays that miss the image.
-__device__ __forceinline__ bool fan_ray_setup(const FanGeom &g, long long r, RayWalk &w) {
+// Walk set-up of ray r = view * np + bin, computed; false for rays that miss the image.
+__device__ __forceinline__ bool fan_ray_setup_compute(const FanGeom &g, long long r, RayWalk &w) {
     const int p = (int)(r % g.np), v = (int)(r / g.np);
     const double2 tr = g.trig_d[v];
     const double sb = tr.x, cb = tr.y;
@@ -55,6 +55,29 @@ __device__ __forceinline__ bool fan_ray_setup(const FanGeom &g, long long r, Ray
     d[2] = 0.0;
     const double ires[3] = {g.ires[0], g.ires[1], 1.0}, ext[3] = {g.ext[0], g.ext[1], 1.0};
     return siddon_setup(src, d, n, res, ires, ext, w);
+}
+
+// Walk set-up of ray r: from the geometry's set-up table when it has one (the
+// same values, stored once per plan), else computed.
+__device__ __forceinline__ bool fan_ray_setup(const FanGeom &g, long long r, RayWalk &w) {
+    if (!g.ray_tab) return fan_ray_setup_compute(g, r, w);
+    const float4 *q = reinterpret_cast<const float4 *>(g.ray_tab + r);
+    const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+    const int flags = __float_as_int(q2.z);
+    const float inf = __int_as_float(0x7f800000);
+    w.a0 = q0.x; w.a1 = q0.y; w.a2 = inf;
+    w.n0 = q0.x; w.n1 = q0.y; w.n2 = inf;
+    w.d0 = q0.z; w.d1 = q0.w; w.d2 = 0.0f;
+    w.k0 = w.k1 = w.k2 = 0.0f;
+    w.L = q1.x;
+    w.scale = q1.y;
+    w.idx = __float_as_int(q1.z);
+    w.nseg = __float_as_int(q1.w);
+    w.s0 = __float_as_int(q2.x);
+    w.s1 = __float_as_int(q2.y);
+    w.s2 = 0;
+    w.grazing = (flags & 2) != 0;
+    return (flags & 1) != 0;
 }
 
 // Line integral of ray r = view * np + bin; sets `grazing` for rays the FP64

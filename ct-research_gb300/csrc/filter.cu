@@ -32,13 +32,13 @@ namespace ct {
 namespace {
 
 constexpr int FT = 256;
-// measured at 256^3 FDK (360 x 384 rows of 512): 2 / 4 / 8 outputs per thread
-// 10.47 / 8.90 / 9.00 ms; one output per thread (two tap loads per product) 11.75 ms
-#ifndef CT_FILTER_FJ
-#define CT_FILTER_FJ 4
-#endif
-constexpr int FJ = CT_FILTER_FJ;   // consecutive outputs per thread
+// Consecutive outputs per thread: 4 where the rows fill the GPU (measured at
+// 256^3 FDK, 360 x 384 rows of 512: 2 / 4 / 8 outputs per thread 10.47 / 8.90 /
+// 9.00 ms against 11.75 with one), else 1 (a 2D scan of a few hundred rows keeps
+// more threads per row: 360 rows of 512, 0.23 ms with 1 against 0.28 with 4).
+constexpr int FJ_WIDE = 4;
 
+template <int FJ>
 __global__ void __launch_bounds__(FT)
 row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restrict__ out) {
     extern __shared__ float sm[];
@@ -162,15 +162,24 @@ row_filter_kernel(const RowFilter f, const float *__restrict__ R, float *__restr
 
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st) {
     CT_REQUIRE(f.np >= 2, "row filter: at least 2 detector samples");
-    const size_t smem = sizeof(float) * (size_t)(4 * f.np - 1 + FJ);
+    const int wide = f.nrow >= 8 * sm_count();
+    const int fj = wide ? FJ_WIDE : 1;
+    const size_t smem = sizeof(float) * (size_t)(4 * f.np - 1 + fj);
     CT_REQUIRE(smem <= 200 * 1024, "row filter: detector row too long for shared memory");
-    if (smem > 48 * 1024)
-        CT_CUDA(cudaFuncSetAttribute(row_filter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                "row_filter smem attribute");
-    // FJ outputs per thread over a P-tile (launch order) or the row, so no thread idles
+    if (smem > 48 * 1024) {
+        if (wide)
+            CT_CUDA(cudaFuncSetAttribute(row_filter_kernel<FJ_WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem),
+                    "row_filter smem attribute");
+        else
+            CT_CUDA(cudaFuncSetAttribute(row_filter_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "row_filter smem attribute");
+    }
+    // fj outputs per thread over a P-tile (launch order) or the row, so no thread idles
     const int span = (f.launch_order && f.w) ? f.tile : f.np;
-    const int block = std::min(FT, std::max(32, ((span + FJ - 1) / FJ + 31) / 32 * 32));
-    row_filter_kernel<<<f.nrow, block, smem, st>>>(f, R, out);
+    const int block = std::min(FT, std::max(32, ((span + fj - 1) / fj + 31) / 32 * 32));
+    if (wide) row_filter_kernel<FJ_WIDE><<<f.nrow, block, smem, st>>>(f, R, out);
+    else row_filter_kernel<1><<<f.nrow, block, smem, st>>>(f, R, out);
     CT_LAUNCH_CHECK("row_filter_kernel");
     return CT_OK;
 }

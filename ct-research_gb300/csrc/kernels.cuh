@@ -25,7 +25,20 @@ struct FanGeom {
     // near-boundary recompute, so that it runs no FP64
     double ires[2], ext[2];
     float2 res_ff[2], hsize_ff[2], D_ff, ipint_ff;
+    // the walk set-up of every ray (fan_ray_table_launch), or null: computed per ray
+    const struct FanRay *ray_tab;
 };
+
+// The forward walk's set-up of one 2D ray, as the FP64 slab test makes it
+// (siddon.cuh): first crossings and steps per axis, exit parameter, |d|,
+// entry pixel, segment count, index steps and flags (bit 0 hit, bit 1 grazing).
+struct __align__(16) FanRay {
+    float a0t, a0s, dat, das;
+    float L, scale;
+    int idx, nseg;
+    int st, ss, flags, pad_;
+};
+static_assert(sizeof(FanRay) == 48, "FanRay: 48 bytes");
 
 inline float2 ff_split_host(double x) {
     const float h = (float)x;
@@ -137,6 +150,8 @@ int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const flo
                    int zt0 = 0, int nzt = 0);
 int cone_bp_ztile();
 int row_filter_launch(const RowFilter &f, const float *R, float *out, cudaStream_t st);
+// The set-up table of every ray of g (nb * np records), for g.ray_tab.
+int fan_ray_table_launch(const FanGeom &g, FanRay *tab, cudaStream_t st);
 int fan_fp_launch(const FanGeom &g, const float *img, void *out, const float *b, const float *rowsum,
                   float eps, double *norms, int mode, const GrazeList &gl, cudaStream_t st);
 int fan_bp_launch(const FanGeom &g, const float *R, float *img, int wmode, const float *colsum, float eps,
