@@ -720,10 +720,14 @@ static int fan_plan_make(ct_fan_plan **out, int nt, int ns, const double size2[2
 
 // The forward walk's set-up table of a plan (48 bytes per ray), built once the
 // geometry is final, synchronously (no later launch or graph capture can
-// precede it).  The one-call drop-ins skip it and set rays up per call.
+// precede it).  The one-call drop-ins skip it and set rays up per call, as
+// does a sinogram whose table would pass kFanRayTableMax.
+constexpr size_t kFanRayTableMax = size_t(4) << 30;
 static int fan_ray_table(ct_fan_plan *pl) {
     const FanGeom &g = pl->g;
-    int s = pl->rays.ensure(sizeof(FanRay) * (size_t)g.nb * g.np);
+    const size_t bytes = sizeof(FanRay) * (size_t)g.nb * g.np;
+    if (bytes > kFanRayTableMax) return CT_OK;
+    int s = pl->rays.ensure(bytes);
     if (s || (s = fan_ray_table_launch(g, pl->rays.as<FanRay>(), nullptr))) return s;
     CT_CUDA(cudaStreamSynchronize(nullptr), "ray set-up table");
     pl->g.ray_tab = pl->rays.as<FanRay>();
