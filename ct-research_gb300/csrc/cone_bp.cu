@@ -54,7 +54,12 @@ namespace {
 #define CT_BP_MINB_FDK 3
 #endif
 constexpr int BP_BX = 32;          // t per block
-constexpr int BP_BY = 4;           // s per block
+// s rows per block (warps of 32 t).  Chord weighting at 512^3 / 360 views,
+// 128 registers: 4 rows 54.6 ms, 2 rows 55.1, 1 row 56.6, 8 rows 57.4.
+#ifndef CT_BP_BY
+#define CT_BP_BY 4
+#endif
+constexpr int BP_BY = CT_BP_BY;    // s per block
 constexpr int BP_ZC = CT_BP_ZC;    // z per thread (register accumulators)
 static_assert(BP_ZC >= 1 && BP_ZC <= 64, "cone_bp: 1 to 64 z per thread");
 // bit k: z0 + k of the thread takes the view
@@ -215,25 +220,25 @@ cone_bp_kernel(const ConeGeom g, const float4 *__restrict__ Q, int v0, int nv, c
     const ff it2 = ff_from((ti + 0.5) * g.res[0] - 0.5 * g.size[0]);
     const ff is2 = ff_from((si + 0.5) * g.res[1] - 0.5 * g.size[1]);
     const ff iz02 = ff_from((z0 + 0.5) * g.res[2] - 0.5 * g.size[2]);
-    const ff D2 = ff_from(g.D), rz2 = ff_from(g.res[2]);
-    const ff ipint2 = ff_from(1.0 / (double)g.pint);
-    const ff xq2 = ff_from((double)g.xsgn / (double)g.xint);   // row quotient per mm of xi
-    const ff p02 = {g.p0, 0.0f}, x02 = {g.x0, 0.0f};
+    const ff D2 = {g.bp_D.x, g.bp_D.y};
+    const ff ipint2 = {g.bp_ipint.x, g.bp_ipint.y};
+    const ff xq2 = {g.bp_xq.x, g.bp_xq.y};   // row quotient per mm of xi
+    const ff p02 = {g.p0, 0.0f};
     // the view-independent factors of the row quotient: (iz lr - xi0) xq = lr (iz xq) - xi0 xq
-    const ff rzxq2 = ff_mul(rz2, xq2), iz0xq2 = ff_mul(iz02, xq2), x0xq2 = ff_mul(x02, xq2);
+    const ff rzxq2 = {g.bp_rzxq.x, g.bp_rzxq.y}, iz0xq2 = ff_mul(iz02, xq2), x0xq2 = {g.bp_x0xq.x, g.bp_x0xq.y};
 
-    const float rz = (float)g.res[2];
+    const float rz = g.bp_rz;
     const float it = it2.hi, is = is2.hi;
-    const float D = (float)g.D;
-    const float ipint = 1.0f / g.pint;
-    const float ht = 0.5f * (float)g.res[0], hs = 0.5f * (float)g.res[1], hz = 0.5f * rz;
-    const float czf = (float)(0.5 * g.size[2]);
-    const float x_base = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);   // iz at z = 0
-    const float iz0 = iz02.hi;                                         // iz of this thread's first z
+    const float D = g.bp_Df;
+    const float ipint = g.bp_ipintf;
+    const float ht = g.bp_ht, hs = g.bp_hs, hz = g.bp_hz;
+    const float czf = g.bp_czf;
+    const float x_base = g.bp_xbase;   // iz at z = 0
+    const float iz0 = iz02.hi;         // iz of this thread's first z
     // largest |iz| of the thread's z range: decides whether z faces can limit the chord
     const float izmax = fmaxf(fabsf(iz0), fabsf(fmaf((float)(BP_ZC - 1), rz, iz0)));
     const float iz_vol = fabsf(x_base);   // largest |iz| of the volume
-    const float irz = 1.0f / rz, iD = 1.0f / D;
+    const float irz = g.bp_irz, iD = g.bp_iD;
     const long long vstride = (long long)g.nx * g.np;
 
     float acc[BP_ZC];
@@ -424,12 +429,14 @@ int cone_bp_launch(const ConeGeom &g, const float4 *Q, int v0, int nv, const flo
     const int ntiles = (g.nz + BP_ZC - 1) / BP_ZC;
     if (nzt <= 0) nzt = ntiles - zt0;
     CT_REQUIRE(zt0 >= 0 && nzt > 0 && zt0 + nzt <= ntiles, "cone_bp: z tile range out of bounds");
+    ConeGeom gk = g;   // with the set-up's constants
+    cone_bp_consts(gk);
     dim3 block(BP_BX, BP_BY);
     dim3 grid((g.nt + BP_BX - 1) / BP_BX, (g.ns + BP_BY - 1) / BP_BY, nzt);
     const size_t smem = sizeof(float2) * (size_t)g.nx;
     CT_REQUIRE(smem <= 48 * 1024, "cone_bp: at most 6144 detector rows");
 #define CT_BP_CASE(W, U)                                                                     \
-    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(g, Q, v0, nv, prev, out, colsum, eps, lambda, lo, hi, zt0)
+    cone_bp_kernel<W, U><<<grid, block, smem, st>>>(gk, Q, v0, nv, prev, out, colsum, eps, lambda, lo, hi, zt0)
     if (update) {
         if (weighting == W_CHORD) CT_BP_CASE(W_CHORD, true);
         else if (weighting == W_FDK_ZERO) CT_BP_CASE(W_FDK_ZERO, true);

@@ -1,5 +1,7 @@
 // cone_geom.cuh -- cone-beam geometry shared by the cone kernels.
 #pragma once
+#include <cmath>
+
 #include "ct_common.cuh"
 
 namespace ct {
@@ -50,6 +52,14 @@ struct ConeGeom {
     // read the same copy of the volume.  A chunk's views are contiguous in the
     // sinogram: a chunk can be projected and copied out on its own.
     const int *vorder;
+    // Float-float (hi, lo) constants of the backprojector, set by
+    // cone_bp_consts: D, res_z * xq, xi[0] * xq and 1 / PInt, where
+    // xq = xsgn / XigamaInt is the row quotient per mm of xi.  Kernel
+    // parameters, so the set-up reads them without holding registers.
+    float2 bp_D, bp_rzxq, bp_x0xq, bp_ipint, bp_xq;
+    // and its float constants: res_z, 1 / res_z, half voxel (t, s, z), size_z / 2,
+    // iz at z = 0, D, 1 / D, 1 / PInt
+    float bp_rz, bp_irz, bp_ht, bp_hs, bp_hz, bp_czf, bp_xbase, bp_Df, bp_iD, bp_ipintf;
 };
 
 // The scalar constants derived from the sizes and the voxel pitch (ext, extf,
@@ -63,6 +73,43 @@ inline void cone_geom_derive(ConeGeom &g) {
     }
     g.srcz = 0.5 * g.size[2];
     g.srczf = (float)g.srcz;
+}
+
+// Host float-float helpers for cone_bp_consts, with the operations of
+// ffloat.cuh's ff_from and ff_mul (each rounded once), so that the constants
+// equal what a kernel would compute from the same doubles.
+inline float2 ff_from_host(double x) {
+    const float h = (float)x;
+    return make_float2(h, (float)(x - (double)h));
+}
+inline float2 ff_mul_host(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = std::fma(a.x, b.x, -p);
+    e = std::fma(a.x, b.y, e);
+    e = std::fma(a.y, b.x, e);
+    const float s = p + e;
+    return make_float2(s, e - (s - p));
+}
+
+// The backprojector's float-float constants (bp_*) from D, res, xsgn, xint,
+// x0 and pint; call after any of them changes.
+inline void cone_bp_consts(ConeGeom &g) {
+    const float2 xq = ff_from_host((double)g.xsgn / (double)g.xint);
+    g.bp_xq = xq;
+    g.bp_D = ff_from_host(g.D);
+    g.bp_rzxq = ff_mul_host(ff_from_host(g.res[2]), xq);
+    g.bp_x0xq = ff_mul_host(make_float2(g.x0, 0.0f), xq);
+    g.bp_ipint = ff_from_host(1.0 / (double)g.pint);
+    g.bp_rz = (float)g.res[2];
+    g.bp_irz = 1.0f / g.bp_rz;
+    g.bp_ht = 0.5f * (float)g.res[0];
+    g.bp_hs = 0.5f * (float)g.res[1];
+    g.bp_hz = 0.5f * g.bp_rz;
+    g.bp_czf = (float)(0.5 * g.size[2]);
+    g.bp_xbase = (float)(0.5 * g.res[2] - 0.5 * g.size[2]);
+    g.bp_Df = (float)g.D;
+    g.bp_iD = 1.0f / g.bp_Df;
+    g.bp_ipintf = 1.0f / g.pint;
 }
 
 }  // namespace ct
