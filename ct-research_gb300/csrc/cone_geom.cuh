@@ -91,8 +91,8 @@ inline float2 ff_mul_host(float2 a, float2 b) {
     return make_float2(s, e - (s - p));
 }
 
-// The backprojector's float-float constants (bp_*) from D, res, xsgn, xint,
-// x0 and pint; call after any of them changes.
+// The backprojector's constants (bp_*) from D, res, size, xsgn, xint, x0 and
+// pint; cone_bp_launch sets them on its copy of the geometry before each launch.
 inline void cone_bp_consts(ConeGeom &g) {
     const float2 xq = ff_from_host((double)g.xsgn / (double)g.xint);
     g.bp_xq = xq;
